@@ -1,0 +1,428 @@
+#!/usr/bin/env python3
+"""bench.py -- GTEPS of delta-stepping SSSP on GB300.
+
+Default workload (the published GPU configuration): R-MAT scale 22, edge
+factor 16, a/b/c/d = .57/.19/.19/.05, symmetrised and deduplicated, uint32
+weights uniform in [1, 255], 64 sources drawn with seed 7, each timed
+separately; delta = max weight / average out-degree.  One step = one SSSP
+from the next source (plain fixed-delta delta-stepping, one cooperative
+persistent launch).  Inputs are synthetic (seeded generator in the library).
+
+  value  = sum(edges reached) / sum(device time of the steps)  [GTEPS]
+           device time = CUDA events around reset + kernel + output unpack,
+           graph resident in HBM
+  e2e    = same metric through gbs_sssp with pinned HOST output buffers
+           (device->host copy of dist + pred inside the timed call)
+
+Multi-GPU: one process per GPU (torchrun); every rank runs the whole workload
+on its own GPU (replicas: a single SSSP does not shard); value = sum over
+ranks / max time.  ``--impl reference`` times the reference's own CPU code.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "rmat22": dict(kind="rmat", scale=22, edgefactor=16, seed=1, wtype="u32", sources=64, source_seed=7),
+    "rmat20": dict(kind="rmat", scale=20, edgefactor=16, seed=1, wtype="u32", sources=64, source_seed=7),
+    "rmat16": dict(kind="rmat", scale=16, edgefactor=16, seed=1, wtype="u32", sources=64, source_seed=7),
+    "rmat24": dict(kind="rmat", scale=24, edgefactor=16, seed=1, wtype="u32", sources=8, source_seed=7),
+    "grid4096": dict(kind="grid", rows=4096, cols=4096, seed=3, wtype="f32", sources=1, source_seed=0),
+    "grid1024": dict(kind="grid", rows=1024, cols=1024, seed=3, wtype="f32", sources=1, source_seed=0),
+}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_workload(gb, wl):
+    if wl["kind"] == "rmat":
+        g = gb.gen_rmat(wl["scale"], wl["edgefactor"], wl["seed"], wl["wtype"])
+        srcs = gb.sample_sources(g, wl["sources"], wl["source_seed"])
+    else:
+        g = gb.gen_grid(wl["rows"], wl["cols"], wl["seed"], wl["wtype"])
+        srcs = np.zeros(1, dtype=np.uint32)
+    return g, srcs
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    rec = d.get(f"{kernel}:{workload}")
+    return rec
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_group(world, rank):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline_port(g, srcs, delta, budget_s: float):
+    """The oracle's C restatement of the reference's serial run_sspath_arr
+    (kind "port"), one thread, on whole single-source runs of this workload
+    until the budget is spent (at least one)."""
+    import oracle
+    done, edges, t_total = 0, 0, 0.0
+    deg = np.diff(g.row.astype(np.int64))
+    while done < len(srcs) and (done == 0 or t_total < budget_s):
+        s = int(srcs[done])
+        t0 = time.perf_counter()
+        d, _ = oracle.delta_stepping(g.row, g.col, g.w, s, delta)
+        t_total += time.perf_counter() - t0
+        edges += int(deg[np.isfinite(d)].sum())
+        done += 1
+    return {"value": edges / t_total / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+            "sample": f"{done} source(s) of this workload, whole SSSP each, oracle restatement of "
+                      f"run_sspath_arr (serial), {t_total:.1f} s"}
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(args):
+    world, rank, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = init_group(world, rank)
+    import runpy
+    runpy.run_path(str(ROOT / "graphbench_gb300" / "build.py"))["build"]()
+    import graphbench_gb300 as gb
+    if not gb.device_available():
+        raise SystemExit("no usable GPU")
+    wl = WORKLOADS[args.workload]
+    t0 = time.time()
+    hg, srcs = make_workload(gb, wl)
+    log(f"[rank {rank}] generated {args.workload}: n={hg.n} m={hg.m} in {time.time() - t0:.1f}s")
+    t0 = time.time()
+    g = gb.Graph.from_host(hg)
+    log(f"[rank {rank}] uploaded in {time.time() - t0:.1f}s")
+    delta = args.delta if args.delta else None
+    light = args.light if args.light is not None else None
+    K, W = args.steps, args.warmup
+    order = [int(srcs[i % len(srcs)]) for i in range(W + K)]
+    dd = gb.DeviceBuffer(4 * hg.n)
+    pd = gb.DeviceBuffer(4 * hg.n)
+    for i in range(W):
+        g.sssp_device(order[i], dd.ptr, pd.ptr, delta=delta, light=light)
+    gb.synchronize()
+    sampler = ClockSampler(local if world > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    sampler.start()
+    barrier(dist)
+    gb.synchronize()
+    wall0 = time.perf_counter()
+    per = []
+    for i in range(W, W + K):
+        st = g.sssp_device(order[i], dd.ptr, pd.ptr, delta=delta, light=light)
+        per.append(st)
+    gb.synchronize()
+    barrier(dist)
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    dev_s = sum(s["device_ms"] for s in per) / 1e3
+    ker_s = sum(s["kernel_ms"] for s in per) / 1e3
+    edges = sum(s["edges_reached"] for s in per)
+    verts = sum(s["reached"] for s in per)
+    # e2e: the public call with pinned host outputs (dist + pred copied back)
+    hd = gb.PinnedBuffer(hg.n, g.dist_dtype)
+    hp = gb.PinnedBuffer(hg.n, np.int32)
+    ke = min(K, args.e2e_steps)
+    e2e_t, e2e_edges = 0.0, 0
+    for i in range(ke):
+        t = time.perf_counter()
+        _, _, st = g.sssp(order[W + i], delta=delta, light=light, out_dist=hd.array, out_pred=hp.array)
+        e2e_t += time.perf_counter() - t
+        e2e_edges += st["edges_reached"]
+    # whole-job aggregates
+    dev_max = allreduce_max(dist, dev_s)
+    wall_max = allreduce_max(dist, wall)
+    edges_all = allreduce_sum(dist, float(edges))
+    e2e_max = allreduce_max(dist, e2e_t)
+    e2e_edges_all = allreduce_sum(dist, float(e2e_edges))
+    result = None
+    if rank == 0:
+        peak, peak_src = measured_peaks()
+        algo_bytes = 16.0 * edges + 24.0 * verts           # per-launch sum over the K launches
+        achieved = algo_bytes / ker_s / 1e9
+        st0 = per[0]
+        traffic = profiled_traffic("sssp_persistent", args.workload)
+        wlc = dict(wl)
+        wlc.update(n=hg.n, m=hg.m, delta=st0["delta_used"], light=st0["light_used"],
+                   blocks=st0["blocks"], source_rule="seeded sample of vertices with out-degree > 0"
+                   if wl["kind"] == "rmat" else "corner vertex 0",
+                   l2=f"inputs larger than L2: CSR {(hg.m * 8 + hg.n * 4) / 1e9:.2f} GB vs 0.135 GB L2; "
+                      "per-step device time from CUDA events on the library's stream",
+                   avg_buckets=sum(s["buckets"] for s in per) / K,
+                   avg_phases=sum(s["phases"] for s in per) / K,
+                   avg_kernel_ms=ker_s * 1e3 / K,
+                   avg_device_ms=dev_s * 1e3 / K,
+                   wall_ms_per_step=wall * 1e3 / K)
+        result = {
+            "metric": "GTEPS SSSP (plain fixed-delta delta-stepping)",
+            "value": edges_all / dev_max / 1e9,
+            "unit": "GTEPS",
+            "n_gpus": world,
+            "steps": K,
+            "warmup": W,
+            "ms_per_step": dev_max * 1e3 / K,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": wl["wtype"],
+            "data": "synthetic (seeded R-MAT / grid generator, no dataset)",
+            "config": {"workload": f"{args.workload}_{wl['wtype']}", **wlc,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
+                         if peak_src == "measured" else "fallback 6.8 TB/s",
+                         "kernel": "sssp_persistent",
+                         "algorithmic_bytes_per_launch": algo_bytes / K,
+                         "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                         "traffic_source": traffic.get("source") if traffic else None},
+            "e2e": {"value": e2e_edges_all / e2e_max / 1e9, "unit": "GTEPS",
+                    "h2d_bytes_per_step": 4,
+                    "d2h_bytes_per_step": hg.n * 8 + 1024,
+                    "steps": ke,
+                    "path": "gbs_sssp (C ABI) -> pinned host dist + pred; graph resident"},
+            "gpu_launches": 4 * K,
+            "clocks": clocks,
+            "wall_ms_per_step": wall_max * 1e3 / K,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            try:
+                result["cpu_baseline"] = cpu_baseline_port(hg, srcs, st0["delta_used"], args.cpu_budget_s)
+            except Exception as e:  # pragma: no cover
+                result["cpu_baseline"] = {"value": None, "unavailable": str(e)}
+    dd.free()
+    pd.free()
+    hd.free()
+    hp.free()
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    if result is not None:
+        print(json.dumps(result), flush=True)
+
+
+# ------------------------------------------------------------ reference arm
+def _ref_worker(args_tuple):
+    """Runs in a forked child: one reference run_sspath_arr, returns
+    (edges_reached, seconds)."""
+    import oracle
+    row, col, w, src, delta, maxd = args_tuple
+    d, secs = oracle.ref_sssp_arr(row, col, w, src, delta, maxdist=maxd, cap_mult=2.0)
+    deg = np.diff(row.astype(np.int64))
+    return int(deg[np.isfinite(d)].sum()), secs
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import oracle
+    from oracle import build_ref, gen
+    try:
+        if not oracle.ref_available("serial"):
+            build_ref.stage()
+            build_ref.compile_ref()
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {e}"}))
+        return
+    wl = WORKLOADS[args.workload]
+    # Bounded sample: the reference's serial run_sspath_arr costs ~120 s per
+    # source at scale 20 on one core (measured), so each step runs one source
+    # per host core on the same R-MAT family at --ref-scale (default 16, the
+    # reference's own CPU-runnable configuration).
+    scale = args.ref_scale if wl["kind"] == "rmat" else None
+    if scale is None:
+        print(json.dumps({"impl": "reference", "unavailable": "reference arm implemented for the R-MAT workloads"}))
+        return
+    row, col, w = gen.rmat(scale, wl["edgefactor"], wl["seed"], wl["wtype"])
+    srcs = gen.sample_sources(row, 64, wl["source_seed"])
+    delta = gen.heuristic_delta(row, w)
+    maxd = 0.0
+    for s in srcs[:4]:
+        dj = oracle.dijkstra(row, col, w, int(s))
+        maxd = max(maxd, float(dj[dj != 0xFFFFFFFF].max()))
+    maxd *= 1.5
+    cores = max(1, min(os.cpu_count() or 1, args.ref_procs))
+    ctx = mp.get_context("fork")
+    K, W = args.steps, args.warmup
+    i = 0
+
+    def one_step(pool):
+        nonlocal i
+        batch = [(row, col, w, int(srcs[(i + j) % len(srcs)]), delta, maxd) for j in range(cores)]
+        i += cores
+        t0 = time.perf_counter()
+        res = pool.map(_ref_worker, batch)
+        return sum(r[0] for r in res), time.perf_counter() - t0
+
+    budget = args.ref_budget_s
+    with ctx.Pool(cores) as pool:
+        for _ in range(min(W, 1)):
+            one_step(pool)
+        done, edges, secs = 0, 0, 0.0
+        t_start = time.perf_counter()
+        while done < K and (done == 0 or time.perf_counter() - t_start < budget):
+            e, s = one_step(pool)
+            edges += e
+            secs += s
+            done += 1
+    val = edges / secs / 1e9
+    sample = (f"{done} step(s) x {cores} concurrent single-source runs of the reference's serial "
+              f"run_sspath_arr (patched D1/D2/D4, logging off) on R-MAT scale {scale} (same generator, "
+              f"edge factor, weights, delta rule and source seed as {args.workload}); stand-in size because "
+              f"one scale-{wl.get('scale')} run takes minutes on one core")
+    print(json.dumps({
+        "impl": "reference", "metric": "GTEPS SSSP (plain fixed-delta delta-stepping)", "value": val,
+        "unit": "GTEPS", "n_gpus": world, "steps": done, "warmup": min(W, 1), "ms_per_step": secs * 1e3 / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference doubles)",
+        "data": "synthetic", "config": {"workload": f"{args.workload}_{wl['wtype']}", "reference_scale": scale,
+                                        "delta": delta, "processes": cores},
+        "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": cores, "kind": "reference", "sample": sample},
+        "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="rmat22")
+    ap.add_argument("--delta", type=float, default=0.0)
+    ap.add_argument("--light", type=float, default=None)
+    ap.add_argument("--e2e-steps", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--ref-scale", type=int, default=16)
+    ap.add_argument("--ref-procs", type=int, default=16)
+    ap.add_argument("--ref-budget-s", type=float, default=120.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,376 @@
+"""graphbench_gb300 -- GB300-native delta-stepping SSSP (Python host side).
+
+Thin ctypes layer over ``libgbsssp.so`` (the C ABI declared in
+``include/gbsssp.h``), mirroring the reference's SSSP entry points
+(``run_sspath_arr`` sssp/csr_sspath_array.c:149, ``run_sspath``
+sssp/csr_sspath.c:38) and its CSR (``t_csr`` include/graph.h:113-127).
+
+The compute path is the CUDA library; there is no CPU fallback.  Loading the
+package does not need a GPU, but any SSSP call raises ``GbsError`` with
+status ``UNSUPPORTED`` (or a CUDA error) when no usable GPU is present, and
+``ImportError`` is raised if the shared library has not been built
+(``python -m graphbench_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libgbsssp.so"
+
+STATUS = {
+    0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "NO_MEMORY", 4: "CAPACITY",
+    5: "TIMEOUT", 6: "OVERFLOW", 7: "UNSUPPORTED", 8: "INTERNAL",
+}
+W_U32, W_F32 = 0, 1
+F_NO_STATS = 0x1
+
+# Every symbol include/gbsssp.h declares (tests check the library exports them).
+EXPORTS = [
+    "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
+    "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
+    "gbs_sssp_multi", "gbs_host_alloc", "gbs_host_free", "gbs_device_alloc", "gbs_device_free",
+    "gbs_device_synchronize",
+    "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
+]
+
+
+class GbsError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str = ""):
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+        super().__init__(f"{where}: {self.name}" + (f" ({msg})" if msg else ""))
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
+                ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
+                ("big_threshold", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double),
+                ("reached", ctypes.c_uint64), ("edges_reached", ctypes.c_uint64),
+                ("improvements", ctypes.c_uint64), ("buckets", ctypes.c_uint32),
+                ("phases", ctypes.c_uint32), ("pending_scans", ctypes.c_uint32),
+                ("blocks", ctypes.c_uint32), ("delta_used", ctypes.c_double),
+                ("light_used", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HostCsr(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("m", ctypes.c_uint64),
+                ("row_offsets", ctypes.POINTER(ctypes.c_uint64)),
+                ("cols", ctypes.POINTER(ctypes.c_uint32)),
+                ("weights", ctypes.c_void_p), ("wtype", ctypes.c_int)]
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m graphbench_gb300.build`")
+    L = ctypes.CDLL(str(LIB_PATH))
+    P = ctypes.c_void_p
+    L.gbs_status_string.restype = ctypes.c_char_p
+    L.gbs_last_error.restype = ctypes.c_char_p
+    L.gbs_graph_create.argtypes = [ctypes.c_uint32, ctypes.c_uint64, P, P, P, ctypes.c_int,
+                                   ctypes.POINTER(P)]
+    L.gbs_graph_destroy.argtypes = [P]
+    L.gbs_graph_info.argtypes = [P, P, P, P, P, P]
+    L.gbs_sssp.argtypes = [P, ctypes.c_uint32, ctypes.POINTER(Params), P, P, ctypes.POINTER(Stats)]
+    L.gbs_sssp_device.argtypes = [P, ctypes.c_uint32, ctypes.POINTER(Params), P, P,
+                                  ctypes.POINTER(Stats)]
+    L.gbs_sssp_multi.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, P,
+                                 ctypes.POINTER(Stats)]
+    L.gbs_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
+    L.gbs_host_free.argtypes = [P]
+    L.gbs_device_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
+    L.gbs_device_free.argtypes = [P]
+    L.gbs_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
+                               ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.POINTER(HostCsr))]
+    L.gbs_gen_grid.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
+                               ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.POINTER(HostCsr))]
+    L.gbs_sample_sources.argtypes = [ctypes.POINTER(HostCsr), ctypes.c_uint32, ctypes.c_uint64, P, P]
+    L.gbs_host_csr_free.argtypes = [ctypes.POINTER(HostCsr)]
+    return L
+
+
+lib = _load()
+
+
+def _check(status: int, where: str) -> None:
+    if status != 0:
+        raise GbsError(status, where, lib.gbs_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_available() -> bool:
+    return bool(lib.gbs_device_available())
+
+
+class DeviceBuffer:
+    """cudaMalloc'd bytes owned by Python (outputs of Graph.sssp_device)."""
+
+    def __init__(self, nbytes: int):
+        p = ctypes.c_void_p()
+        _check(lib.gbs_device_alloc(nbytes, ctypes.byref(p)), "gbs_device_alloc")
+        self.ptr, self.nbytes = p, nbytes
+
+    def free(self) -> None:
+        if self.ptr:
+            lib.gbs_device_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host array (fast device-to-host copies)."""
+
+    def __init__(self, count: int, dtype):
+        dtype = np.dtype(dtype)
+        p = ctypes.c_void_p()
+        _check(lib.gbs_host_alloc(max(1, count * dtype.itemsize), ctypes.byref(p)), "gbs_host_alloc")
+        self.ptr = p
+        buf = (ctypes.c_char * max(1, count * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=count)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            lib.gbs_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def synchronize() -> None:
+    _check(lib.gbs_device_synchronize(), "gbs_device_synchronize")
+
+
+# ------------------------------------------------------------ generators
+@dataclass
+class HostGraph:
+    """A CSR in host memory: exclusive uint64 offsets, uint32 columns,
+    uint32 or float32 weights."""
+    row: np.ndarray
+    col: np.ndarray
+    w: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return len(self.row) - 1
+
+    @property
+    def m(self) -> int:
+        return int(self.row[-1])
+
+
+def _take_host_csr(p) -> HostGraph:
+    c = p.contents
+    n, m = int(c.n), int(c.m)
+    row = np.ctypeslib.as_array(c.row_offsets, shape=(n + 1,)).copy()
+    col = np.ctypeslib.as_array(c.cols, shape=(max(m, 1),))[:m].copy()
+    wt = np.float32 if c.wtype == W_F32 else np.uint32
+    wp = ctypes.cast(c.weights, ctypes.POINTER(ctypes.c_float if wt is np.float32 else ctypes.c_uint32))
+    w = np.ctypeslib.as_array(wp, shape=(max(m, 1),))[:m].copy()
+    lib.gbs_host_csr_free(p)
+    return HostGraph(row, col, w)
+
+
+def gen_rmat(scale: int, edgefactor: int = 16, seed: int = 1, wtype: str = "u32",
+             wmin: int = 1, wmax: int = 255) -> HostGraph:
+    p = ctypes.POINTER(HostCsr)()
+    _check(lib.gbs_gen_rmat(scale, edgefactor, seed, W_F32 if wtype == "f32" else W_U32,
+                            wmin, wmax, ctypes.byref(p)), "gbs_gen_rmat")
+    return _take_host_csr(p)
+
+
+def gen_grid(rows: int, cols: int, seed: int = 3, wtype: str = "f32",
+             wmin: int = 1, wmax: int = 255) -> HostGraph:
+    p = ctypes.POINTER(HostCsr)()
+    _check(lib.gbs_gen_grid(rows, cols, seed, W_F32 if wtype == "f32" else W_U32,
+                            wmin, wmax, ctypes.byref(p)), "gbs_gen_grid")
+    return _take_host_csr(p)
+
+
+def sample_sources(g: HostGraph, count: int, seed: int) -> np.ndarray:
+    hc = HostCsr(g.n, g.m, g.row.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                 g.col.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                 g.w.ctypes.data, W_F32 if g.w.dtype == np.float32 else W_U32)
+    out = np.zeros(count, dtype=np.uint32)
+    got = np.zeros(1, dtype=np.uint32)
+    _check(lib.gbs_sample_sources(ctypes.byref(hc), count, seed, _ptr(out), _ptr(got)),
+           "gbs_sample_sources")
+    return out[: int(got[0])]
+
+
+def heuristic_delta(g: HostGraph) -> float:
+    """max_w / average out-degree."""
+    if g.m == 0:
+        return 1.0
+    return float(np.max(g.w)) / (g.m / g.n)
+
+
+# ----------------------------------------------------------------- graph
+class Graph:
+    """A device-resident CSR (gbs_graph).  Replaces the t_csr that
+    scan_csr_idx/read_graph_csr or read_csr_bin build (graph/csr.c)."""
+
+    def __init__(self, row, col, w):
+        row = np.ascontiguousarray(row, dtype=np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        w = np.ascontiguousarray(w)
+        if w.dtype == np.float32:
+            self.wtype = W_F32
+        elif w.dtype == np.uint32:
+            self.wtype = W_U32
+        else:
+            raise TypeError("weights must be uint32 or float32")
+        self.n = len(row) - 1
+        self.m = int(row[-1]) if len(row) else 0
+        self.dist_dtype = np.float32 if self.wtype == W_F32 else np.uint32
+        h = ctypes.c_void_p()
+        _check(lib.gbs_graph_create(self.n, len(col), _ptr(row), _ptr(col), _ptr(w), self.wtype,
+                                    ctypes.byref(h)), "gbs_graph_create")
+        self._h = h
+
+    @classmethod
+    def from_host(cls, g: HostGraph) -> "Graph":
+        return cls(g.row, g.col, g.w)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.gbs_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def info(self) -> dict:
+        n, m, wt, mw, dd = (ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_int(), ctypes.c_double(),
+                            ctypes.c_double())
+        _check(lib.gbs_graph_info(self._h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(wt),
+                                  ctypes.byref(mw), ctypes.byref(dd)), "gbs_graph_info")
+        return {"n": n.value, "m": m.value, "wtype": wt.value, "max_weight": mw.value,
+                "default_delta": dd.value}
+
+    @staticmethod
+    def params(delta: float | None = None, light: float | None = None, flags: int = 0,
+               wait_limit_ms: int = 0, big_threshold: int = 0) -> Params:
+        return Params(float(delta) if delta else 0.0, float(light) if light is not None else -1.0,
+                      flags, wait_limit_ms, big_threshold, 0)
+
+    def sssp(self, source: int, delta: float | None = None, light: float | None = None,
+             out_dist: np.ndarray | None = None, out_pred: np.ndarray | None = None,
+             want_dist: bool = True, want_pred: bool = True, **kw):
+        """One SSSP; returns (dist, pred, stats dict).  dist is uint32
+        (UINT32_MAX unreached) or float32 (+inf unreached); pred is int32
+        (pred[source] = source, -1 unreached)."""
+        p = self.params(delta, light, **kw)
+        st = Stats()
+        dist = out_dist if out_dist is not None else (np.empty(self.n, dtype=self.dist_dtype) if want_dist else None)
+        pred = out_pred if out_pred is not None else (np.empty(self.n, dtype=np.int32) if want_pred else None)
+        _check(lib.gbs_sssp(self._h, int(source), ctypes.byref(p),
+                            _ptr(dist) if dist is not None else None,
+                            _ptr(pred) if pred is not None else None, ctypes.byref(st)), "gbs_sssp")
+        return dist, pred, st.as_dict()
+
+    def sssp_device(self, source: int, dist_ptr: int | None = None, pred_ptr: int | None = None,
+                    delta: float | None = None, light: float | None = None, **kw) -> dict:
+        """Run with outputs left in caller-owned device memory (raw pointers)."""
+        p = self.params(delta, light, **kw)
+        st = Stats()
+        _check(lib.gbs_sssp_device(self._h, int(source), ctypes.byref(p), dist_ptr, pred_ptr,
+                                   ctypes.byref(st)), "gbs_sssp_device")
+        return st.as_dict()
+
+    def sssp_multi(self, sources, delta: float | None = None, light: float | None = None,
+                   want_dist: bool = True, want_pred: bool = False, **kw):
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        k = len(src)
+        p = self.params(delta, light, **kw)
+        st = Stats()
+        dist = np.empty((k, self.n), dtype=self.dist_dtype) if want_dist else None
+        pred = np.empty((k, self.n), dtype=np.int32) if want_pred else None
+        _check(lib.gbs_sssp_multi(self._h, _ptr(src), k, ctypes.byref(p),
+                                  _ptr(dist) if dist is not None else None,
+                                  _ptr(pred) if pred is not None else None, ctypes.byref(st)),
+               "gbs_sssp_multi")
+        return dist, pred, st.as_dict()
+
+
+# ------------------------------------------------ reference-shaped mirror
+@dataclass
+class TCsr:
+    """Python mirror of the reference's t_csr (include/graph.h:113-127):
+    vet_idx[v] is the INCLUSIVE end offset of row v (row v starts at
+    vet_idx[v-1], 0 for v = 0), edge_idx the targets, edge_weight the doubles
+    of edge_info[].edge_weight, and weight (vet_info[].weight) receives the
+    distances."""
+    vet_idx: np.ndarray
+    edge_idx: np.ndarray
+    edge_weight: np.ndarray
+    weight: np.ndarray | None = None
+
+    @property
+    def v_size(self) -> int:
+        return len(self.vet_idx)
+
+
+def _tcsr_to_graph(gs: TCsr) -> Graph:
+    ends = np.asarray(gs.vet_idx, dtype=np.int64)
+    row = np.zeros(len(ends) + 1, dtype=np.uint64)
+    row[1:] = ends
+    w = np.asarray(gs.edge_weight, dtype=np.float64)
+    if np.all(w == np.floor(w)) and (len(w) == 0 or (w.min() >= 0 and w.max() < 2**32 - 1)):
+        return Graph(row, gs.edge_idx, w.astype(np.uint32))
+    w32 = w.astype(np.float32)
+    if not np.array_equal(w32.astype(np.float64), w):
+        raise GbsError(7, "run_sspath_arr", "fractional double weights that are not exactly float32")
+    return Graph(row, gs.edge_idx, w32)
+
+
+def run_sspath_arr(gs: TCsr, source: int, delta: float) -> np.ndarray:
+    """Mirror of run_sspath_arr(gs, predecesor, source, delta)
+    (sssp/csr_sspath_array.c:149): fills gs.weight with float64 distances
+    (inf for unreached) and returns them.  Integer weights run on the uint32
+    path (exact in double); float32-representable weights on the float32
+    path."""
+    with _tcsr_to_graph(gs) as g:
+        dist, _, _ = g.sssp(int(source), delta=float(delta), want_pred=False)
+    out = dist.astype(np.float64)
+    if g.wtype == W_U32:
+        out[dist == np.uint32(0xFFFFFFFF)] = math.inf
+    gs.weight = out
+    return out

@@ -1,0 +1,543 @@
+// gbs_api.cu -- the C ABI of libgbsssp (include/gbsssp.h): graph upload,
+// workspace, launch sequence of one SSSP run, error reporting.
+//
+// One run on the graph's stream:
+//   [mid]   first-heavy-edge index per row, only when the light split changes
+//   reset   dp = unreached, tag = none, control block, source in ring bucket 0
+//   persistent cooperative kernel (gbs_sssp_kernel.cuh)
+//   unpack  dp -> dist / pred in the caller's layout
+//   [stats] reached vertices and edges (the GTEPS numerator)
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gbs_sssp_kernel.cuh"
+
+using namespace gbs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gbs_status fail(gbs_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define GBS_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(e_ == cudaErrorMemoryAllocation ? GBS_ERR_NO_MEMORY : GBS_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+    } while (0)
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_mid(const uint32_t *__restrict__ row, const uint2 *__restrict__ adj, uint32_t n,
+                      uint32_t light_bits, uint32_t *__restrict__ mid) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t lo = row[v], hi = row[v + 1];
+        while (lo < hi) {  // first edge with weight > light
+            const uint32_t m = lo + ((hi - lo) >> 1);
+            if (adj[m].y <= light_bits) lo = m + 1;
+            else hi = m;
+        }
+        mid[v] = lo;
+    }
+}
+
+__global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restrict__ tag, uint32_t n,
+                        uint32_t src, uint32_t *__restrict__ ring0, Ctl *ctl) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        dp[v] = (v == src) ? (unsigned long long)src : kUnreached;   // dist 0, pred = src
+        tag[v] = (v == src) ? 0u : kTagInit;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ring0[0] = src;
+        ctl->ring_cnt[0] = 1;
+        ctl->pend_min[0] = kTagInit;
+        ctl->pend_min[1] = kTagInit;
+        ctl->mode = kPhLightFirst;
+        ctl->next_bucket = 0;
+    }
+}
+
+template <bool F32>
+__global__ void k_unpack(const unsigned long long *__restrict__ dp, uint32_t n, uint32_t src,
+                         uint32_t *__restrict__ dist, int32_t *__restrict__ pred) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const unsigned long long x = dp[v];
+        const bool reached = x != kUnreached;
+        if (dist) dist[v] = reached ? (uint32_t)(x >> 32) : (F32 ? 0x7F800000u : 0xFFFFFFFFu);
+        if (pred) pred[v] = reached ? (v == src ? (int32_t)src : (int32_t)(uint32_t)x) : -1;
+    }
+}
+
+__global__ void k_stats(const unsigned long long *__restrict__ dp, const uint32_t *__restrict__ row,
+                        uint32_t n, Ctl *ctl) {
+    unsigned long long r = 0, e = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        if (dp[v] != kUnreached) {
+            ++r;
+            e += row[v + 1] - row[v];
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(0xffffffffu, r, o);
+        e += __shfl_down_sync(0xffffffffu, e, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (r) atomicAdd(&ctl->st_reached, r);
+        if (e) atomicAdd(&ctl->st_edges_reached, e);
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- graph
+struct gbs_graph {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    gbs_weight_type wtype = GBS_WEIGHT_U32;
+    double max_w = 0.0;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    uint32_t *d_row = nullptr;
+    uint2 *d_adj = nullptr;
+    // workspace
+    bool ws_ready = false;
+    Workspace ws{};
+    uint32_t *d_dist = nullptr;
+    int32_t *d_pred = nullptr;
+    uint32_t mid_light_bits = 0;
+    bool mid_valid = false;
+    uint32_t epoch = 1, hround = 1;
+    int blocks = 0;
+    Ctl host_ctl{};
+};
+
+namespace {
+
+void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits, uint32_t n,
+               std::vector<uint2> &adj) {
+    unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::atomic<uint32_t> next{0};
+    const uint32_t grain = 4096;
+    auto worker = [&]() {
+        std::vector<uint64_t> keys;
+        for (;;) {
+            const uint32_t v0 = next.fetch_add(grain);
+            if (v0 >= n) break;
+            const uint32_t v1 = std::min<uint64_t>((uint64_t)v0 + grain, n);
+            for (uint32_t v = v0; v < v1; ++v) {
+                const uint64_t b = row[v], e = row[v + 1];
+                keys.resize(e - b);
+                for (uint64_t i = b; i < e; ++i) keys[i - b] = ((uint64_t)wbits[i] << 32) | cols[i];
+                std::sort(keys.begin(), keys.end());
+                for (uint64_t i = b; i < e; ++i)
+                    adj[i] = make_uint2((uint32_t)keys[i - b], (uint32_t)(keys[i - b] >> 32));
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+}
+
+gbs_status ensure_workspace(gbs_graph *g) {
+    if (g->ws_ready) return GBS_OK;
+    const size_t n = g->n ? g->n : 1;
+    Workspace &w = g->ws;
+    GBS_CUDA(cudaMalloc(&w.dp, sizeof(unsigned long long) * n));
+    GBS_CUDA(cudaMalloc(&w.tag, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&w.fst, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&w.hst, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&w.mid, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&w.ring, sizeof(uint32_t) * n * kNB));
+    GBS_CUDA(cudaMalloc(&w.fq, sizeof(uint32_t) * n * 3));
+    GBS_CUDA(cudaMalloc(&w.S, sizeof(uint32_t) * n * 2));
+    GBS_CUDA(cudaMalloc(&w.pend, sizeof(uint32_t) * n * 2));
+    // one frontier holds each vertex at most once, so one phase pushes at most
+    // sum(len/kChunk + 1) <= 2m/kChunk chunks (rows split only if len >= kChunk)
+    const uint64_t cap = 2 * g->m / kChunk + 64;
+    w.big_cap = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFF0ull);
+    GBS_CUDA(cudaMalloc(&w.big, sizeof(uint4) * (size_t)w.big_cap * 2));
+    GBS_CUDA(cudaMalloc(&w.ctl, sizeof(Ctl)));
+    GBS_CUDA(cudaMalloc(&g->d_dist, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&g->d_pred, sizeof(int32_t) * n));
+    GBS_CUDA(cudaMemsetAsync(w.fst, 0, sizeof(uint32_t) * n, g->stream));
+    GBS_CUDA(cudaMemsetAsync(w.hst, 0, sizeof(uint32_t) * n, g->stream));
+    g->epoch = 1;
+    g->hround = 1;
+    int per_sm = 0;
+    const void *kfn = g->wtype == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<true>
+                                                 : (const void *)sssp_persistent<false>;
+    GBS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kTPB, 0));
+    if (per_sm < 1) return fail(GBS_ERR_UNSUPPORTED, "persistent kernel cannot be resident");
+    g->blocks = per_sm * g->sms;
+    g->ws_ready = true;
+    return GBS_OK;
+}
+
+void free_graph(gbs_graph *g) {
+    if (!g) return;
+    cudaFree(g->d_row);
+    cudaFree(g->d_adj);
+    Workspace &w = g->ws;
+    cudaFree(w.dp); cudaFree(w.tag); cudaFree(w.fst); cudaFree(w.hst); cudaFree(w.mid);
+    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.big); cudaFree(w.ctl);
+    cudaFree(g->d_dist);
+    cudaFree(g->d_pred);
+    for (auto &e : g->ev) if (e) cudaEventDestroy(e);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+struct Resolved {
+    double delta, light;
+    uint32_t delta_u, light_bits;
+    float inv_delta_f;
+};
+
+double default_delta(const gbs_graph *g) {
+    if (g->m == 0 || g->n == 0) return 1.0;
+    const double avg = (double)g->m / (double)g->n;
+    const double d = g->max_w / avg;
+    return d > 0 ? d : 1.0;
+}
+
+Resolved resolve(const gbs_graph *g, const gbs_params *p) {
+    Resolved r{};
+    double delta = (p && p->delta > 0) ? p->delta : default_delta(g);
+    double light = (p && p->light >= 0) ? p->light : -1.0;
+    if (g->wtype == GBS_WEIGHT_U32) {
+        double fd = std::floor(delta);
+        r.delta_u = (uint32_t)std::min(std::max(fd, 1.0), 4294967295.0);
+        r.delta = r.delta_u;
+        if (light < 0) light = r.delta;
+        const double fl = std::floor(light);
+        r.light_bits = (uint32_t)std::min(std::max(fl, 0.0), 4294967295.0);
+        r.light = r.light_bits;
+        r.inv_delta_f = 0.f;
+    } else {
+        r.delta = delta;
+        r.inv_delta_f = (float)(1.0 / delta);
+        if (light < 0) light = delta;
+        float lf = (float)light;
+        if ((double)lf > light) lf = std::nextafter(lf, -INFINITY);
+        if (lf < 0) lf = 0;
+        if (std::isinf(lf)) lf = 3.4028234663852886e38f;
+        uint32_t bits;
+        std::memcpy(&bits, &lf, 4);
+        r.light_bits = bits;
+        r.light = lf;
+        r.delta_u = 1;
+    }
+    return r;
+}
+
+gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t *dist_dev,
+                      int32_t *pred_dev, gbs_stats *stats) {
+    if (src >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
+    gbs_status st = ensure_workspace(g);
+    if (st != GBS_OK) return st;
+    const Resolved r = resolve(g, p);
+    cudaStream_t s = g->stream;
+    const int tb = 256;
+    const int eb = std::max(1, std::min<int>((g->n + tb - 1) / tb, g->sms * 8));
+    if (!g->mid_valid || g->mid_light_bits != r.light_bits) {
+        k_mid<<<eb, tb, 0, s>>>(g->d_row, g->d_adj, g->n, r.light_bits, g->ws.mid);
+        GBS_CUDA(cudaGetLastError());
+        g->mid_light_bits = r.light_bits;
+        g->mid_valid = true;
+    }
+    if (g->epoch > 0xF0000000u || g->hround > 0xF0000000u) {
+        GBS_CUDA(cudaMemsetAsync(g->ws.fst, 0, sizeof(uint32_t) * g->n, s));
+        GBS_CUDA(cudaMemsetAsync(g->ws.hst, 0, sizeof(uint32_t) * g->n, s));
+        g->epoch = 1;
+        g->hround = 1;
+    }
+    SsspArgs a{};
+    a.g.n = g->n;
+    a.g.m = g->m;
+    a.g.wtype = g->wtype;
+    a.g.row = g->d_row;
+    a.g.adj = g->d_adj;
+    a.ws = g->ws;
+    a.source = src;
+    a.epoch0 = g->epoch;
+    a.hround0 = g->hround;
+    a.delta_u = r.delta_u;
+    a.inv_delta_f = r.inv_delta_f;
+    a.big_threshold = (p && p->big_threshold) ? std::max<uint32_t>(p->big_threshold, kChunk) : 2048u;
+    a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
+    a.flags = p ? p->flags : 0u;
+    a.run_ns = a.wait_ns * 16ull;
+
+    GBS_CUDA(cudaEventRecord(g->ev[0], s));
+    GBS_CUDA(cudaMemsetAsync(g->ws.ctl, 0, sizeof(Ctl), s));
+    k_reset<<<eb, tb, 0, s>>>(g->ws.dp, g->ws.tag, g->n, src, g->ws.ring, g->ws.ctl);
+    GBS_CUDA(cudaGetLastError());
+    GBS_CUDA(cudaEventRecord(g->ev[1], s));
+    void *args[] = {&a};
+    const void *kfn = g->wtype == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<true>
+                                                 : (const void *)sssp_persistent<false>;
+    GBS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(g->blocks), dim3(kTPB), args, 0, s));
+    GBS_CUDA(cudaEventRecord(g->ev[2], s));
+    if (dist_dev || pred_dev) {
+        if (g->wtype == GBS_WEIGHT_F32)
+            k_unpack<true><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, dist_dev, pred_dev);
+        else
+            k_unpack<false><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, dist_dev, pred_dev);
+        GBS_CUDA(cudaGetLastError());
+    }
+    GBS_CUDA(cudaEventRecord(g->ev[3], s));
+    const bool want_stats = !(p && (p->flags & GBS_F_NO_STATS));
+    if (want_stats) {
+        k_stats<<<eb, tb, 0, s>>>(g->ws.dp, g->d_row, g->n, g->ws.ctl);
+        GBS_CUDA(cudaGetLastError());
+    }
+    GBS_CUDA(cudaMemcpyAsync(&g->host_ctl, g->ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    GBS_CUDA(cudaStreamSynchronize(s));
+    const Ctl &c = g->host_ctl;
+    g->epoch = c.err_info + 1;
+    g->hround = c.pad4 + 1;
+    if (c.error != kErrNone) {
+        // stamps of an aborted run are unknown: start over next time
+        g->epoch = 0xF0000001u;
+        switch (c.error) {
+            case kErrTimeout: return fail(GBS_ERR_TIMEOUT, "device-side wait limit exceeded");
+            case kErrCapacity: return fail(GBS_ERR_CAPACITY, "device work list overflow");
+            case kErrOverflow: return fail(GBS_ERR_OVERFLOW, "uint32 path sum overflow");
+            default: return fail(GBS_ERR_INTERNAL, "device error");
+        }
+    }
+    if (stats) {
+        float ms = 0.f;
+        std::memset(stats, 0, sizeof(*stats));
+        GBS_CUDA(cudaEventElapsedTime(&ms, g->ev[0], g->ev[3]));
+        stats->device_ms = ms;
+        GBS_CUDA(cudaEventElapsedTime(&ms, g->ev[1], g->ev[2]));
+        stats->kernel_ms = ms;
+        stats->reached = want_stats ? c.st_reached : 0;
+        stats->edges_reached = want_stats ? c.st_edges_reached : 0;
+        stats->improvements = c.st_improvements;
+        stats->buckets = c.st_buckets;
+        stats->phases = c.st_phases;
+        stats->pending_scans = c.st_pending_scans;
+        stats->blocks = (uint32_t)g->blocks;
+        stats->delta_used = r.delta;
+        stats->light_used = r.light;
+    }
+    return GBS_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char *gbs_status_string(gbs_status s) {
+    switch (s) {
+        case GBS_OK: return "ok";
+        case GBS_ERR_INVALID_ARG: return "invalid argument";
+        case GBS_ERR_CUDA: return "CUDA error";
+        case GBS_ERR_NO_MEMORY: return "out of memory";
+        case GBS_ERR_CAPACITY: return "device work list capacity exceeded";
+        case GBS_ERR_TIMEOUT: return "device wait limit exceeded";
+        case GBS_ERR_OVERFLOW: return "uint32 distance overflow";
+        case GBS_ERR_UNSUPPORTED: return "unsupported";
+        case GBS_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+const char *gbs_last_error(void) { return g_last_error.c_str(); }
+
+int gbs_abi_version(void) { return GBS_ABI_VERSION; }
+
+int gbs_device_available(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    int dev = 0, major = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess) return 0;
+    return major >= 10 ? 1 : 0;
+}
+
+gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets, const uint32_t *cols,
+                            const void *weights, gbs_weight_type wtype, gbs_graph **out) {
+    if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!row_offsets || (m && (!cols || !weights)))
+        return fail(GBS_ERR_INVALID_ARG, "NULL CSR array");
+    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32)
+        return fail(GBS_ERR_INVALID_ARG, "unknown weight type");
+    if (n == 0 || n > 0x7FFFFFFFu) return fail(GBS_ERR_INVALID_ARG, "vertex count must be in [1, 2^31)");
+    if (m >= 0xFFFFFFFFull) return fail(GBS_ERR_UNSUPPORTED, "edge count must be < 2^32");
+    if (row_offsets[0] != 0 || row_offsets[n] != m)
+        return fail(GBS_ERR_INVALID_ARG, "row_offsets must start at 0 and end at m");
+    for (uint32_t v = 0; v < n; ++v)
+        if (row_offsets[v + 1] < row_offsets[v]) return fail(GBS_ERR_INVALID_ARG, "row_offsets decrease");
+    std::vector<uint32_t> wbits(m);
+    double max_w = 0.0;
+    for (uint64_t e = 0; e < m; ++e) {
+        if (cols[e] >= n) return fail(GBS_ERR_INVALID_ARG, "column index out of range");
+        if (wtype == GBS_WEIGHT_U32) {
+            const uint32_t w = ((const uint32_t *)weights)[e];
+            wbits[e] = w;
+            if (w > max_w) max_w = w;
+        } else {
+            float w = ((const float *)weights)[e];
+            if (!(w >= 0.0f) || std::isinf(w))
+                return fail(GBS_ERR_INVALID_ARG, "float32 weights must be finite and >= 0");
+            if (w == 0.0f) w = 0.0f;  // -0.0 -> +0.0
+            std::memcpy(&wbits[e], &w, 4);
+            if (w > max_w) max_w = w;
+        }
+    }
+    int dev = 0;
+    GBS_CUDA(cudaGetDevice(&dev));
+    gbs_graph *g = new gbs_graph();
+    g->n = n;
+    g->m = m;
+    g->wtype = wtype;
+    g->max_w = max_w;
+    g->device = dev;
+    cudaError_t e;
+    if ((e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        free_graph(g);
+        return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (auto &ev : g->ev) {
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+            free_graph(g);
+            return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    std::vector<uint2> adj(m);
+    sort_rows(row_offsets, cols, wbits.data(), n, adj);
+    std::vector<uint32_t> row32(n + 1);
+    for (uint32_t v = 0; v <= n; ++v) row32[v] = (uint32_t)row_offsets[v];
+    if ((e = cudaMalloc(&g->d_row, sizeof(uint32_t) * (n + 1))) != cudaSuccess ||
+        (e = cudaMalloc(&g->d_adj, sizeof(uint2) * (m ? m : 1))) != cudaSuccess ||
+        (e = cudaMemcpy(g->d_row, row32.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
+        (m && (e = cudaMemcpy(g->d_adj, adj.data(), sizeof(uint2) * m, cudaMemcpyHostToDevice)) !=
+                  cudaSuccess)) {
+        free_graph(g);
+        return fail(e == cudaErrorMemoryAllocation ? GBS_ERR_NO_MEMORY : GBS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = g;
+    return GBS_OK;
+}
+
+gbs_status gbs_graph_destroy(gbs_graph *g) {
+    if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    cudaStreamSynchronize(g->stream);
+    free_graph(g);
+    return GBS_OK;
+}
+
+gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m, gbs_weight_type *wtype,
+                          double *max_weight, double *def_delta) {
+    if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+    if (wtype) *wtype = g->wtype;
+    if (max_weight) *max_weight = g->max_w;
+    if (def_delta) *def_delta = default_delta(g);
+    return GBS_OK;
+}
+
+gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_dev,
+                           int32_t *pred_dev, gbs_stats *stats) {
+    if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    return launch_run(g, source, params, (uint32_t *)dist_dev, pred_dev, stats);
+}
+
+gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_out,
+                    int32_t *pred_out, gbs_stats *stats) {
+    if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    gbs_status st = ensure_workspace(g);
+    if (st != GBS_OK) return st;
+    st = launch_run(g, source, params, dist_out ? g->d_dist : nullptr, pred_out ? g->d_pred : nullptr,
+                    stats);
+    if (st != GBS_OK) return st;
+    if (dist_out)
+        GBS_CUDA(cudaMemcpyAsync(dist_out, g->d_dist, sizeof(uint32_t) * g->n, cudaMemcpyDeviceToHost,
+                                 g->stream));
+    if (pred_out)
+        GBS_CUDA(cudaMemcpyAsync(pred_out, g->d_pred, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost,
+                                 g->stream));
+    GBS_CUDA(cudaStreamSynchronize(g->stream));
+    return GBS_OK;
+}
+
+gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_params *params,
+                          void *dist_out, int32_t *pred_out, gbs_stats *stats) {
+    if (!g || (k && !sources)) return fail(GBS_ERR_INVALID_ARG, "NULL argument");
+    gbs_stats total{};
+    for (uint32_t i = 0; i < k; ++i) {
+        gbs_stats one{};
+        void *d = dist_out ? (void *)((uint32_t *)dist_out + (size_t)i * g->n) : nullptr;
+        int32_t *pr = pred_out ? pred_out + (size_t)i * g->n : nullptr;
+        gbs_status st = gbs_sssp(g, sources[i], params, d, pr, &one);
+        if (st != GBS_OK) return st;
+        total.device_ms += one.device_ms;
+        total.kernel_ms += one.kernel_ms;
+        total.reached += one.reached;
+        total.edges_reached += one.edges_reached;
+        total.improvements += one.improvements;
+        total.buckets += one.buckets;
+        total.phases += one.phases;
+        total.pending_scans += one.pending_scans;
+        total.blocks = one.blocks;
+        total.delta_used = one.delta_used;
+        total.light_used = one.light_used;
+    }
+    if (stats) *stats = total;
+    return GBS_OK;
+}
+
+gbs_status gbs_host_alloc(size_t bytes, void **out) {
+    if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
+    GBS_CUDA(cudaMallocHost(out, bytes ? bytes : 1));
+    return GBS_OK;
+}
+
+gbs_status gbs_host_free(void *p) {
+    GBS_CUDA(cudaFreeHost(p));
+    return GBS_OK;
+}
+
+gbs_status gbs_device_alloc(size_t bytes, void **out) {
+    if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
+    GBS_CUDA(cudaMalloc(out, bytes ? bytes : 1));
+    return GBS_OK;
+}
+
+gbs_status gbs_device_free(void *p) {
+    GBS_CUDA(cudaFree(p));
+    return GBS_OK;
+}
+
+gbs_status gbs_device_synchronize(void) {
+    GBS_CUDA(cudaDeviceSynchronize());
+    return GBS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,137 @@
+// gbs_internal.cuh -- device data layout and helpers shared by the SSSP
+// kernels of libgbsssp (sm_103a).
+//
+// HBM layout of one resident graph (built once by gbs_graph_create):
+//   row[n+1]  uint32  exclusive row offsets (m < 2^32)
+//   adj[m]    uint2   {col, weight bits}; each row sorted by (weight, col), so
+//                     the light edges of any split w <= L are a row prefix
+//   mid[n]    uint32  first heavy edge of each row for the cached split L
+// Per-run state (workspace, reused across runs on the same graph):
+//   dp[n]     uint64  (dist bits << 32) | pred; ~0 = unreached.  Non-negative
+//                     float32 bit patterns order like the values, so one 64-bit
+//                     atomicMin updates distance and predecessor together and
+//                     keeps the smallest predecessor among equal distances.
+//   tag[n]    uint32  smallest bucket the vertex was queued for (ring dedup)
+//   fst[n]    uint32  frontier stamp (dedup inside one light sub-phase)
+//   hst[n]    uint32  heavy-round stamp (dedup of the settled list S)
+//   ring      NB lists of n uint32: bucket b lives in list b % NB while it is
+//                     inside the window [W, W + NB)
+//   fq        3 lists of n uint32: current-bucket frontier, rotated per phase
+//   S         2 lists of n uint32: vertices settled in the current bucket
+//   pend      2 lists of n uint32: vertices whose bucket is beyond the window
+//   big       2 lists of chunk descriptors for very long edge lists
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gbsssp.h"
+
+namespace gbs {
+
+constexpr int kNB = 64;                 // ring buckets (window width)
+constexpr uint32_t kTagInit = 0xFFFFFFFFu;
+constexpr uint32_t kTagPending = 0xFFFFFFFEu;
+constexpr uint32_t kBucketMax = 0xFFFFFF00u;
+constexpr unsigned long long kUnreached = ~0ull;
+constexpr uint32_t kChunk = 512;        // edges per big-list chunk
+constexpr int kTPB = 512;               // threads per CTA of the persistent kernel
+
+enum ErrCode : uint32_t {
+    kErrNone = 0,
+    kErrTimeout = 1,
+    kErrCapacity = 2,
+    kErrOverflow = 3,
+};
+
+enum Mode : uint32_t { kModeBucket = 0, kModePending = 1, kModeDone = 2 };
+
+// Control block in global memory.  Barrier words sit on their own 128-byte
+// lines; the rest is read by every CTA after each barrier.
+struct __align__(128) Ctl {
+    uint32_t bar_count;
+    uint32_t pad0[31];
+    uint32_t bar_gen;
+    uint32_t pad1[31];
+    uint32_t error;
+    uint32_t err_info;
+    uint32_t mode;          // decision published by the last CTA at a barrier
+    uint32_t next_bucket;
+    uint32_t pad2[28];
+    uint32_t ring_cnt[kNB];
+    uint32_t fq_cnt[3];
+    uint32_t s_cnt[2];
+    uint32_t pend_cnt[2];
+    uint32_t pend_min[2];
+    uint32_t big_cnt[2];
+    uint32_t pad3[21];
+    // statistics (written by CTA 0 at exit)
+    uint32_t st_buckets;
+    uint32_t st_phases;
+    uint32_t st_pending_scans;
+    uint32_t pad4;
+    unsigned long long st_improvements;
+    unsigned long long st_reached;
+    unsigned long long st_edges_reached;
+};
+
+struct DevGraph {
+    uint32_t n;
+    uint64_t m;
+    gbs_weight_type wtype;
+    const uint32_t *row;
+    const uint2 *adj;
+};
+
+struct Workspace {
+    unsigned long long *dp;
+    uint32_t *tag, *fst, *hst, *mid;
+    uint32_t *ring, *fq, *S, *pend;
+    uint4 *big;
+    uint32_t big_cap;
+    Ctl *ctl;
+};
+
+// Everything the persistent kernel needs, passed by value.
+struct SsspArgs {
+    DevGraph g;
+    Workspace ws;
+    uint32_t source;
+    uint32_t epoch0;        // first frontier stamp of this run
+    uint32_t hround0;       // first heavy-round stamp of this run
+    uint32_t delta_u;       // uint32 bucket width (>= 1)
+    float inv_delta_f;      // float32: bucket = floor(d * inv_delta)
+    uint32_t big_threshold;
+    uint32_t flags;         // GBS_F_* of the call
+    unsigned long long wait_ns;   // limit of one barrier wait
+    unsigned long long run_ns;    // limit of the whole run
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
+    uint2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];"
+                 : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+}  // namespace gbs

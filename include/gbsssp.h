@@ -1,0 +1,190 @@
+/*
+ * gbsssp.h -- native C ABI of the GB300 delta-stepping SSSP library
+ * (libgbsssp.so).  Plain C types only; every call returns a gbs_status.
+ *
+ * It replaces the single-source shortest path of GRAPHBENCH:
+ *   run_sspath_arr(t_csr *gs, p_list *predecesor, lint source, double delta)
+ *       sssp/csr_sspath_array.c:149-151 (declared in no header; called from
+ *       main/main.c:223)
+ *   run_sspath(t_csr *gs, p_list *predecesor, lint source, double delta)
+ *       include/list.h:32-33, sssp/csr_sspath.c:38
+ * over the CSR that graph/csr.c builds (scan_csr_idx/read_graph_csr
+ * include/csr.h:4-5, read_csr_bin include/csr.h:15-16, separate_csr
+ * graph/csr.c:74).  The reference-shaped entry points over t_csr live in
+ * gbsssp_compat.h; this header is the handle-based API underneath them.
+ *
+ * Differences from the reference interface, by design:
+ *   - the graph is uploaded once (gbs_graph_create) and stays resident on the
+ *     GPU; the reference re-splits it into light/heavy copies on every call
+ *     (separate_csr inside run_sspath_arr, :173);
+ *   - errors are status codes, never exit() (the reference's ERROR_PRINT,
+ *     include/graph.h:74);
+ *   - no global state: calls on different graphs are independent; calls on
+ *     the same graph must not overlap (one workspace per graph);
+ *   - distances are computed in the weight type (uint32 or float32) and are
+ *     bit-identical to the least fixpoint (Dijkstra) for any bucket width;
+ *     the predecessor of v is the smallest-id u with dist[u] + w(u,v) ==
+ *     dist[v] (one tight predecessor per vertex, see gbs_sssp).
+ */
+#ifndef GBSSSP_H
+#define GBSSSP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBS_ABI_VERSION 1
+
+typedef enum gbs_status {
+    GBS_OK = 0,
+    GBS_ERR_INVALID_ARG = 1,  /* null pointer, malformed CSR, source out of range */
+    GBS_ERR_CUDA = 2,         /* a CUDA runtime call failed (see gbs_last_error) */
+    GBS_ERR_NO_MEMORY = 3,    /* device or pinned host allocation failed */
+    GBS_ERR_CAPACITY = 4,     /* a device work list would overflow its bound */
+    GBS_ERR_TIMEOUT = 5,      /* a device-side wait ran past its limit */
+    GBS_ERR_OVERFLOW = 6,     /* a uint32 path sum reached 2^32 - 1 */
+    GBS_ERR_UNSUPPORTED = 7,  /* no usable GPU, or a size the build does not handle */
+    GBS_ERR_INTERNAL = 8
+} gbs_status;
+
+typedef enum gbs_weight_type {
+    GBS_WEIGHT_U32 = 0,       /* uint32 weights, uint32 distances (UINT32_MAX = unreached) */
+    GBS_WEIGHT_F32 = 1        /* float32 weights >= 0, float32 distances (+inf = unreached) */
+} gbs_weight_type;
+
+typedef struct gbs_graph gbs_graph;
+
+/* Per-call knobs.  Zero-initialise and set what you need. */
+typedef struct gbs_params {
+    double delta;            /* bucket width; <= 0 selects max_w / average out-degree
+                                (the published configs' rule).  uint32 graphs use
+                                floor(delta), at least 1. */
+    double light;            /* light/heavy split: an edge is light iff w <= light.
+                                < 0 selects light = delta (the reference's rule,
+                                graph/csr.c:84). */
+    uint32_t flags;          /* GBS_F_* */
+    uint32_t wait_limit_ms;  /* device-side wait limit; 0 = 4000 ms */
+    uint32_t big_threshold;  /* edges at or above which one vertex's edge list is
+                                split across the whole GPU; 0 = 2048 */
+    uint32_t reserved;
+} gbs_params;
+
+#define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
+/* Failure-path test: one CTA never arrives at the first grid barrier, so every
+ * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
+ * wait_limit_ms and the device stays usable.  Never set in normal use. */
+#define GBS_F_TEST_STALL 0x80000000u
+
+typedef struct gbs_stats {
+    double device_ms;        /* CUDA-event time of the whole run: reset + kernel + outputs */
+    double kernel_ms;        /* CUDA-event time of the persistent relaxation kernel */
+    uint64_t reached;        /* vertices with a finite distance */
+    uint64_t edges_reached;  /* sum of out-degrees of reached vertices (the GTEPS numerator) */
+    uint64_t improvements;   /* successful distance decreases */
+    uint32_t buckets;        /* buckets processed */
+    uint32_t phases;         /* grid-wide synchronised phases */
+    uint32_t pending_scans;  /* times the far list was re-bucketed */
+    uint32_t blocks;         /* CTAs of the persistent launch */
+    double delta_used;       /* bucket width actually used */
+    double light_used;       /* light/heavy split actually used */
+} gbs_stats;
+
+/* Library / device */
+const char *gbs_status_string(gbs_status s);
+/* Last error message of the calling thread ("" if none). */
+const char *gbs_last_error(void);
+int gbs_abi_version(void);
+/* 1 if a CUDA device of compute capability 10.x or newer is usable, else 0. */
+int gbs_device_available(void);
+
+/*
+ * Graph.  row_offsets has n+1 entries (row v is [row_offsets[v],
+ * row_offsets[v+1])), cols and weights have m entries.  The arrays are host
+ * memory and are copied; the caller keeps ownership.  uint32 weights may be
+ * any value; float32 weights must be finite and >= 0 (-0.0 is read as +0.0).
+ * Parallel edges and self loops are allowed.  Replaces the CSR produced by
+ * scan_csr_idx + read_graph_csr (graph/csr.c:4-202) or read_csr_bin
+ * (graph/csr.c:211-299), which use inclusive int64 end offsets instead.
+ */
+gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
+                            const uint32_t *cols, const void *weights,
+                            gbs_weight_type wtype, gbs_graph **out);
+gbs_status gbs_graph_destroy(gbs_graph *g);
+gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m,
+                          gbs_weight_type *wtype, double *max_weight,
+                          double *default_delta);
+
+/*
+ * One single-source shortest path, outputs in HOST memory (pinned memory from
+ * gbs_host_alloc transfers fastest).  dist_out: n uint32 or float32 values in
+ * the graph's weight type; pred_out: n int32 values (pred[source] = source,
+ * -1 for unreached vertices).  Either output may be NULL.  params and stats
+ * may be NULL.  Replaces run_sspath_arr (sssp/csr_sspath_array.c:149), whose
+ * distances land in gs->vet_info[v].weight as doubles and whose predecessor
+ * argument is never written.
+ */
+gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params,
+                    void *dist_out, int32_t *pred_out, gbs_stats *stats);
+
+/*
+ * Same computation with outputs in DEVICE memory allocated by the caller
+ * (cudaMalloc; n elements each; NULL skips that output).  Results stay on the
+ * GPU; the call returns after the run finished.
+ */
+gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *params,
+                           void *dist_dev, int32_t *pred_dev, gbs_stats *stats);
+
+/*
+ * Many sources over one graph (the source loop of btwcentral/csr_bc.c:40-43).
+ * dist_out / pred_out are host arrays of k*n elements, row i belonging to
+ * sources[i] (either may be NULL).  Each row is identical to what gbs_sssp
+ * returns for that source.
+ */
+gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
+                          const gbs_params *params, void *dist_out, int32_t *pred_out,
+                          gbs_stats *stats);
+
+/* Pinned host memory for fast transfers. */
+gbs_status gbs_host_alloc(size_t bytes, void **out);
+gbs_status gbs_host_free(void *p);
+/* Device memory for gbs_sssp_device outputs (plain cudaMalloc / cudaFree). */
+gbs_status gbs_device_alloc(size_t bytes, void **out);
+gbs_status gbs_device_free(void *p);
+/* Blocks until all work the library queued on the device has finished. */
+gbs_status gbs_device_synchronize(void);
+
+/*
+ * Synthetic inputs (host-side C generators; deterministic for a given seed).
+ * R-MAT: edgefactor * 2^scale samples with a,b,c,d = .57,.19,.19,.05, vertex
+ * ids permuted, self loops dropped, symmetrised, duplicates removed.  Grid:
+ * rows x cols vertices, 4-neighbour, symmetric.  Weights belong to the
+ * undirected pair: uint32 uniform in [wmin, wmax], or float32 uniform in
+ * [1, 1000) on a 2^-14 lattice.  Rows are sorted by column.
+ */
+typedef struct gbs_host_csr {
+    uint32_t n;
+    uint64_t m;
+    uint64_t *row_offsets;   /* n+1 */
+    uint32_t *cols;          /* m */
+    void *weights;           /* m uint32 or float32 */
+    gbs_weight_type wtype;
+} gbs_host_csr;
+
+gbs_status gbs_gen_rmat(uint32_t scale, uint32_t edgefactor, uint64_t seed,
+                        gbs_weight_type wtype, uint32_t wmin, uint32_t wmax,
+                        gbs_host_csr **out);
+gbs_status gbs_gen_grid(uint32_t rows, uint32_t cols, uint64_t seed,
+                        gbs_weight_type wtype, uint32_t wmin, uint32_t wmax,
+                        gbs_host_csr **out);
+/* count distinct vertices of out-degree > 0, drawn with the given seed */
+gbs_status gbs_sample_sources(const gbs_host_csr *g, uint32_t count, uint64_t seed,
+                              uint32_t *out, uint32_t *got);
+void gbs_host_csr_free(gbs_host_csr *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBSSSP_H */

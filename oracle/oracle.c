@@ -1,0 +1,413 @@
+/*
+ * oracle.c -- CPU oracle for the delta-stepping SSSP path.  TEST INFRASTRUCTURE
+ * ONLY: loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg as the checker.  The product library never links or calls it.
+ *
+ * What is restated here (reference paths relative to the GRAPHBENCH tree):
+ *   - or_delta_stepping_{u32,f32}: the serial array delta-stepping of
+ *     sssp/csr_sspath_array.c:149-363 (run_sspath_arr without USE_OMP) with
+ *     its helpers request_arr_single (:941-961), remember_arr_single
+ *     (:1019-1042) and relax_arr_single (:403-449), over the light/heavy split
+ *     of graph/csr.c:74-130 (separate_csr: light iff w <= delta).  Buckets are
+ *     tombstoned arrays with a per-vertex (bucket, position) index
+ *     (include/array.h:3-10).  Defects D1 (vidx rewritten when the vertex does
+ *     not move, :445-446), D2 (b_total not re-incremented when a vertex that
+ *     was already moved to S is re-inserted, :426-434) and D4 (S/R sized by
+ *     the edge count, :202-204) are fixed; D3 (uninitialised degrees) does not
+ *     arise because the split is computed directly.  The distance type is the
+ *     reference's double for uint32 weights (every path sum < 2^53 is exact)
+ *     and float for float32 weights (fl32(d[u] + w) per relaxation).
+ *   - or_dijkstra_{u32,f32}: binary-heap Dijkstra in the weight's own type, an
+ *     independent cross-check of the same least fixpoint (the reference's own
+ *     Dijkstra is sssp/csr_sspath.c:5-36, a list priority queue).
+ *   - or_min_tight_pred_*: predecessor = smallest tight in-neighbour, i.e. the
+ *     one edge the product's packed (dist<<32 | pred) atomicMin keeps.
+ *   - or_count_tight_preds_* / or_fill_tight_preds_*: all tight predecessors,
+ *     the set the list path keeps (sssp/csr_sspath.c:116-118) for betweenness.
+ *
+ * CSR convention: row[v]..row[v+1] (exclusive offsets, uint64), col uint32.
+ * Unreached vertices: dist = UINT32_MAX (u32) / +inf (f32), pred = -1.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#define OR_UNREACHED_U32 0xFFFFFFFFu
+
+/* ------------------------------------------------------------------ heap */
+typedef struct { double key; uint32_t v; } or_hent;
+
+typedef struct {
+    or_hent *a;
+    size_t n, cap;
+} or_heap;
+
+static int heap_push(or_heap *h, double key, uint32_t v) {
+    if (h->n == h->cap) {
+        size_t nc = h->cap ? h->cap * 2 : 1024;
+        or_hent *na = (or_hent *)realloc(h->a, nc * sizeof(or_hent));
+        if (!na) return -1;
+        h->a = na; h->cap = nc;
+    }
+    size_t i = h->n++;
+    while (i > 0) {
+        size_t p = (i - 1) / 2;
+        if (h->a[p].key <= key) break;
+        h->a[i] = h->a[p];
+        i = p;
+    }
+    h->a[i].key = key; h->a[i].v = v;
+    return 0;
+}
+
+static or_hent heap_pop(or_heap *h) {
+    or_hent top = h->a[0];
+    or_hent last = h->a[--h->n];
+    size_t i = 0;
+    for (;;) {
+        size_t c = 2 * i + 1;
+        if (c >= h->n) break;
+        if (c + 1 < h->n && h->a[c + 1].key < h->a[c].key) c++;
+        if (h->a[c].key >= last.key) break;
+        h->a[i] = h->a[c];
+        i = c;
+    }
+    if (h->n) h->a[i] = last;
+    return top;
+}
+
+/* ------------------------------------------------------------- Dijkstra */
+/* Returns 0 on success, 1 if a path sum does not fit in 32 bits, -1 on OOM. */
+int or_dijkstra_u32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                    const uint32_t *w, uint32_t src, uint32_t *dist) {
+    uint64_t *d = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
+    char *done = (char *)calloc(n ? n : 1, 1);
+    or_heap h = {0};
+    int rc = 0;
+    if (!d || !done) { free(d); free(done); return -1; }
+    for (uint32_t v = 0; v < n; v++) d[v] = UINT64_MAX;
+    d[src] = 0;
+    if (heap_push(&h, 0.0, src)) rc = -1;
+    while (!rc && h.n) {
+        or_hent t = heap_pop(&h);
+        uint32_t u = t.v;
+        if (done[u]) continue;
+        done[u] = 1;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint64_t nd = d[u] + w[e];
+            uint32_t v = col[e];
+            if (nd < d[v]) {
+                d[v] = nd;
+                if (heap_push(&h, (double)nd, v)) { rc = -1; break; }
+            }
+        }
+    }
+    for (uint32_t v = 0; v < n && rc >= 0; v++) {
+        if (d[v] == UINT64_MAX) dist[v] = OR_UNREACHED_U32;
+        else if (d[v] >= OR_UNREACHED_U32) { rc = 1; dist[v] = OR_UNREACHED_U32; }
+        else dist[v] = (uint32_t)d[v];
+    }
+    free(h.a); free(d); free(done);
+    return rc;
+}
+
+int or_dijkstra_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                    const float *w, uint32_t src, float *dist) {
+    char *done = (char *)calloc(n ? n : 1, 1);
+    or_heap h = {0};
+    int rc = 0;
+    if (!done) return -1;
+    for (uint32_t v = 0; v < n; v++) dist[v] = INFINITY;
+    dist[src] = 0.0f;
+    if (heap_push(&h, 0.0, src)) rc = -1;
+    while (!rc && h.n) {
+        or_hent t = heap_pop(&h);
+        uint32_t u = t.v;
+        if (done[u]) continue;
+        done[u] = 1;
+        float du = dist[u];
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            volatile float nd = du + w[e]; /* one float32 rounding */
+            uint32_t v = col[e];
+            if (nd < dist[v]) {
+                dist[v] = nd;
+                if (heap_push(&h, (double)nd, v)) { rc = -1; break; }
+            }
+        }
+    }
+    free(h.a); free(done);
+    return rc;
+}
+
+/* --------------------------------------------------------- predecessors */
+int or_min_tight_pred_u32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const uint32_t *w, uint32_t src, const uint32_t *dist,
+                          int32_t *pred) {
+    for (uint32_t v = 0; v < n; v++) pred[v] = -1;
+    for (uint32_t u = 0; u < n; u++) {
+        if (dist[u] == OR_UNREACHED_U32) continue;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint32_t v = col[e];
+            if (v == src) continue;
+            if ((uint64_t)dist[u] + w[e] == (uint64_t)dist[v]) {
+                if (pred[v] < 0 || (uint32_t)pred[v] > u) pred[v] = (int32_t)u;
+            }
+        }
+    }
+    pred[src] = (int32_t)src;
+    return 0;
+}
+
+int or_min_tight_pred_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const float *w, uint32_t src, const float *dist,
+                          int32_t *pred) {
+    for (uint32_t v = 0; v < n; v++) pred[v] = -1;
+    for (uint32_t u = 0; u < n; u++) {
+        if (isinf(dist[u])) continue;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint32_t v = col[e];
+            if (v == src) continue;
+            volatile float nd = dist[u] + w[e];
+            if (nd == dist[v]) {
+                if (pred[v] < 0 || (uint32_t)pred[v] > u) pred[v] = (int32_t)u;
+            }
+        }
+    }
+    pred[src] = (int32_t)src;
+    return 0;
+}
+
+/* Checks that every reached v != src has pred[v] = u with an edge (u, v) such
+ * that dist[u] + w == dist[v] (computed in the weight type), that unreached
+ * vertices have pred -1, and returns the number of violations. */
+int64_t or_check_preds_u32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                           const uint32_t *w, uint32_t src, const uint32_t *dist,
+                           const int32_t *pred) {
+    int64_t bad = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        if (v == src) continue;
+        if (dist[v] == OR_UNREACHED_U32) { bad += (pred[v] != -1); continue; }
+        int32_t p = pred[v];
+        if (p < 0 || (uint32_t)p >= n || dist[p] == OR_UNREACHED_U32) { bad++; continue; }
+        int ok = 0;
+        for (uint64_t e = row[p]; e < row[p + 1]; e++)
+            if (col[e] == v && (uint64_t)dist[p] + w[e] == dist[v]) { ok = 1; break; }
+        bad += !ok;
+    }
+    return bad;
+}
+
+int64_t or_check_preds_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                           const float *w, uint32_t src, const float *dist,
+                           const int32_t *pred) {
+    int64_t bad = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        if (v == src) continue;
+        if (isinf(dist[v])) { bad += (pred[v] != -1); continue; }
+        int32_t p = pred[v];
+        if (p < 0 || (uint32_t)p >= n || isinf(dist[p])) { bad++; continue; }
+        int ok = 0;
+        for (uint64_t e = row[p]; e < row[p + 1]; e++) {
+            volatile float nd = dist[p] + w[e];
+            if (col[e] == v && nd == dist[v]) { ok = 1; break; }
+        }
+        bad += !ok;
+    }
+    return bad;
+}
+
+/* All tight predecessors (one entry per tight edge), grouped by target:
+ * count pass fills cnt[v]; fill pass writes into out at off[v] (exclusive
+ * prefix of cnt) in increasing source order. */
+void or_count_tight_preds_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                              const double *w, uint32_t src, const double *dist,
+                              uint64_t *cnt) {
+    memset(cnt, 0, sizeof(uint64_t) * n);
+    for (uint32_t u = 0; u < n; u++) {
+        if (isinf(dist[u])) continue;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint32_t v = col[e];
+            if (v != src && dist[u] + w[e] == dist[v]) cnt[v]++;
+        }
+    }
+}
+
+void or_fill_tight_preds_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                             const double *w, uint32_t src, const double *dist,
+                             const uint64_t *off, uint64_t *cursor, uint32_t *out) {
+    memcpy(cursor, off, sizeof(uint64_t) * n);
+    for (uint32_t u = 0; u < n; u++) {
+        if (isinf(dist[u])) continue;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint32_t v = col[e];
+            if (v != src && dist[u] + w[e] == dist[v]) out[cursor[v]++] = u;
+        }
+    }
+}
+
+/* ------------------------------------------------- delta-stepping (serial) */
+/* Bucket array: entries are vertex ids, -1 is a tombstone
+ * (structs/array.c:91-96, remove_find_arr).  idx = next free slot,
+ * num = live entries (include/array.h:12-48). */
+typedef struct { int64_t *a; int64_t idx, num, cap; } or_arr;
+
+static int arr_push(or_arr *b, int64_t v) {
+    if (b->idx == b->cap) {
+        int64_t nc = b->cap ? b->cap * 2 : 64;
+        int64_t *na = (int64_t *)realloc(b->a, sizeof(int64_t) * nc);
+        if (!na) return -1;
+        b->a = na; b->cap = nc;
+    }
+    b->a[b->idx++] = v;
+    b->num++;
+    return 0;
+}
+
+typedef struct { int64_t src, dst; double w; } or_req;   /* (src, dst, w) triple */
+typedef struct { or_req *a; int64_t n, cap; } or_reqs;
+
+static int req_push(or_reqs *r, int64_t s, int64_t d, double w) {
+    if (r->n == r->cap) {
+        int64_t nc = r->cap ? r->cap * 2 : 1024;
+        or_req *na = (or_req *)realloc(r->a, sizeof(or_req) * nc);
+        if (!na) return -1;
+        r->a = na; r->cap = nc;
+    }
+    r->a[r->n].src = s; r->a[r->n].dst = d; r->a[r->n].w = w;
+    r->n++;
+    return 0;
+}
+
+typedef struct {
+    or_arr *B;
+    int64_t nb;
+} or_buckets;
+
+static or_arr *bucket_at(or_buckets *bs, int64_t i) {
+    if (i >= bs->nb) {
+        int64_t nn = bs->nb ? bs->nb : 16;
+        while (nn <= i) nn *= 2;
+        or_arr *na = (or_arr *)realloc(bs->B, sizeof(or_arr) * nn);
+        if (!na) return NULL;
+        memset(na + bs->nb, 0, sizeof(or_arr) * (nn - bs->nb));
+        bs->B = na; bs->nb = nn;
+    }
+    return &bs->B[i];
+}
+
+/* DIST_T is the accumulation type; ADD rounds once to DIST_T. */
+#define OR_DS_BODY(DIST_T, WEIGHT_T)                                              \
+    const double delta_recip = 1.0 / delta;                                       \
+    or_buckets bs = {0};                                                          \
+    or_arr S = {0};                                                               \
+    or_reqs R = {0};                                                              \
+    int64_t *vb = (int64_t *)malloc(sizeof(int64_t) * (n ? n : 1));               \
+    int64_t *vp = (int64_t *)malloc(sizeof(int64_t) * (n ? n : 1));               \
+    int rc = 0;                                                                   \
+    if (!vb || !vp) { free(vb); free(vp); return -1; }                            \
+    for (uint32_t v = 0; v < n; v++) { d[v] = (DIST_T)INFINITY; vb[v] = -1; vp[v] = -1; } \
+    /* source goes to B[0] (csr_sspath_array.c:226-230) */                        \
+    if (arr_push(bucket_at(&bs, 0), src)) rc = -1;                                \
+    vb[src] = 0; vp[src] = 0;                                                     \
+    d[src] = (DIST_T)0;                                                           \
+    int64_t b_total = 1, iter = 0;                                                \
+    while (!rc && b_total > 0) {                    /* :237 */                    \
+        or_arr *Bi;                                                               \
+        for (;;) {                                  /* :240 while(B[iter]->num>0) */\
+            Bi = bucket_at(&bs, iter);                                            \
+            if (!Bi) { rc = -1; break; }                                          \
+            if (Bi->num <= 0) break;                                              \
+            /* request_arr_single over the light graph (:941-961) */              \
+            R.n = 0;                                                              \
+            for (int64_t j = 0; j < Bi->idx && !rc; j++) {                        \
+                int64_t q = Bi->a[j];                                             \
+                if (q == -1) continue;                                            \
+                for (uint64_t e = row[q]; e < row[q + 1]; e++)                    \
+                    if ((double)w[e] <= delta)                                    \
+                        if (req_push(&R, q, col[e], (double)w[e])) { rc = -1; break; } \
+            }                                                                     \
+            /* remember_arr_single (:1019-1042) */                                \
+            for (int64_t j = 0; j < Bi->idx && !rc; j++) {                        \
+                int64_t q = Bi->a[j];                                             \
+                if (q == -1) continue;                                            \
+                if (arr_push(&S, q)) { rc = -1; break; }                          \
+                S.num--; /* S counts entries via idx only */                      \
+                Bi->a[j] = -1;                                                    \
+                vb[q] = -1; vp[q] = -1;                                           \
+            }                                                                     \
+            b_total -= Bi->num;                                                   \
+            Bi->idx = 0; Bi->num = 0;                                             \
+            OR_RELAX(DIST_T, WEIGHT_T)                                            \
+        }                                                                         \
+        if (rc) break;                                                            \
+        /* heavy requests over S (:340-349) */                                    \
+        R.n = 0;                                                                  \
+        for (int64_t j = 0; j < S.idx && !rc; j++) {                              \
+            int64_t q = S.a[j];                                                   \
+            for (uint64_t e = row[q]; e < row[q + 1]; e++)                        \
+                if ((double)w[e] > delta)                                         \
+                    if (req_push(&R, q, col[e], (double)w[e])) { rc = -1; break; } \
+        }                                                                         \
+        if (rc) break;                                                            \
+        OR_RELAX(DIST_T, WEIGHT_T)                                                \
+        S.idx = 0; S.num = 0;                       /* empty_arr(S) :351 */       \
+        iter++;                                                                   \
+    }                                                                             \
+    if (phases) *phases = iter;                                                   \
+    for (int64_t i = 0; i < bs.nb; i++) free(bs.B[i].a);                          \
+    free(bs.B); free(S.a); free(R.a); free(vb); free(vp);                         \
+    return rc;
+
+/* relax_arr_single (:403-449) with D1 and D2 fixed.  w is carried as double in
+ * the request (as in the reference's t_arr_elem.double_val) and converted to
+ * the accumulation type before the add. */
+#define OR_RELAX(DIST_T, WEIGHT_T)                                                \
+    for (int64_t i = 0; i < R.n && !rc; i++) {                                    \
+        int64_t s = R.a[i].src, t = R.a[i].dst;                                   \
+        DIST_T ori = d[t];                                                        \
+        volatile DIST_T nv = d[s] + (DIST_T)R.a[i].w;                             \
+        if (nv <= ori) {                                                          \
+            d[t] = nv;                                                            \
+            int64_t nbk = (int64_t)((double)nv * delta_recip);                    \
+            if (!isinf((double)ori)) {                                            \
+                int64_t ob = vb[t];                                               \
+                if (ob != nbk) {                                                  \
+                    if (vp[t] != -1) {                                            \
+                        bs.B[ob].a[vp[t]] = -1;                                   \
+                        bs.B[ob].num--;                                           \
+                    } else {                                                      \
+                        b_total++;              /* D2 fix */                      \
+                    }                                                             \
+                    or_arr *nb_ = bucket_at(&bs, nbk);                            \
+                    if (!nb_ || arr_push(nb_, t)) { rc = -1; break; }             \
+                    vb[t] = nbk; vp[t] = nb_->idx - 1;   /* D1 fix: only on move */ \
+                }                                                                 \
+            } else {                                                              \
+                or_arr *nb_ = bucket_at(&bs, nbk);                                \
+                if (!nb_ || arr_push(nb_, t)) { rc = -1; break; }                 \
+                b_total++;                                                        \
+                vb[t] = nbk; vp[t] = nb_->idx - 1;                                \
+            }                                                                     \
+        }                                                                         \
+    }
+
+/* Returns 0 on success, -1 on allocation failure.  *phases = buckets walked. */
+int or_delta_stepping_u32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const uint32_t *w, uint32_t src, double delta,
+                          double *d, int64_t *phases) {
+    OR_DS_BODY(double, uint32_t)
+}
+
+int or_delta_stepping_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const float *w, uint32_t src, double delta,
+                          float *d, int64_t *phases) {
+    OR_DS_BODY(float, float)
+}
+
+/* Same algorithm over double weights (the reference's own edge type). */
+int or_delta_stepping_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const double *w, uint32_t src, double delta,
+                          double *d, int64_t *phases) {
+    OR_DS_BODY(double, double)
+}

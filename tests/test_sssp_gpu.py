@@ -1,0 +1,183 @@
+"""GPU parity tests: the CUDA path (through the C ABI in libgbsssp.so) against
+the oracle and the committed golden vectors.  Distances must be bit-identical
+(uint32 and float32 alike: the least fixpoint does not depend on the
+relaxation order or the bucket width), and predecessors must equal the
+smallest tight in-neighbour, which the oracle computes independently."""
+import hashlib
+import importlib.util
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).resolve().parent / "golden"
+U32MAX = 0xFFFFFFFF
+KNOWN = json.loads((GOLD / "known_answer.json").read_text())
+SEEDED = json.loads((GOLD / "seeded.json").read_text())
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _mg():
+    spec = importlib.util.spec_from_file_location("make_golden", GOLD / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(gb):
+    assert gb.device_available(), "GPU tests need a CUDA device (compute capability 10.x)"
+
+
+def run_and_check(gb, orc, row, col, w, src, **kw):
+    with gb.Graph(row, col, w) as g:
+        d, p, st = g.sssp(src, **kw)
+    ref = orc.dijkstra(row, col, w, src)
+    assert np.array_equal(d, ref), f"{int(np.sum(d != ref))} distances differ"
+    rp = orc.min_tight_pred(row, col, w, src, ref)
+    assert np.array_equal(p, rp), f"{int(np.sum(p != rp))} predecessors differ"
+    assert orc.check_preds(row, col, w, src, d, p) == 0
+    return d, p, st
+
+
+@pytest.mark.parametrize("case", KNOWN, ids=[c["name"] for c in KNOWN])
+def test_known_answer(case, gb):
+    mg = _mg()
+    row, col, w = mg.to_csr(case)
+    with gb.Graph(row, col, w) as g:
+        d, p, _ = g.sssp(case["source"], delta=case["delta"])
+    assert np.array_equal(d, mg.expected_dist(case))
+    assert p.tolist() == case["pred"]
+
+
+@pytest.mark.parametrize("case", SEEDED, ids=[c["name"] for c in SEEDED])
+def test_seeded_golden(case, gb):
+    mg = _mg()
+    row, col, w, src = mg.make_seeded(case)
+    with gb.Graph(row, col, w) as g:
+        d, p, st = g.sssp(src, delta=case["delta"])
+    assert sha(d) == case["dist_sha"]
+    assert sha(p) == case["pred_sha"]
+    assert st["reached"] == case["reached"]
+    assert st["edges_reached"] == case["edges_reached"]
+
+
+@pytest.mark.parametrize("delta,light", [(None, None), (1, None), (3, None), (40, None), (255, None),
+                                         (10000, None), (8, 0), (8, 64), (2, 300)])
+def test_rmat_deltas_and_splits(delta, light, gb, orc):
+    a = gb.gen_rmat(13, 16, 3)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    run_and_check(gb, orc, a.row, a.col, a.w, src, delta=delta, light=light)
+
+
+def test_rmat16_many_sources_one_graph(gb, orc):
+    """Repeated runs on one resident graph (stamps carried across runs)."""
+    a = gb.gen_rmat(16, 16, 1)
+    srcs = gb.sample_sources(a, 6, 7)
+    with gb.Graph.from_host(a) as g:
+        for s in srcs:
+            d, p, st = g.sssp(int(s))
+            ref = orc.dijkstra(a.row, a.col, a.w, int(s))
+            assert np.array_equal(d, ref)
+            assert np.array_equal(p, orc.min_tight_pred(a.row, a.col, a.w, int(s), ref))
+            assert st["buckets"] >= 1 and st["phases"] >= 2
+
+
+def test_big_rows_split_across_gpu(gb, orc):
+    """A low big_threshold routes hub rows through the shared chunk list."""
+    a = gb.gen_rmat(14, 32, 5)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    run_and_check(gb, orc, a.row, a.col, a.w, src, big_threshold=512)
+    run_and_check(gb, orc, a.row, a.col, a.w, src, big_threshold=512, delta=100000)
+
+
+def test_pending_list_small_delta(gb, orc):
+    """delta = 1 with weights up to 255 pushes vertices past the 64-bucket
+    ring window, exercising the pending list and its re-bucketing."""
+    a = gb.gen_grid(40, 60, 11, "u32")
+    _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, 0, delta=1)
+    assert st["pending_scans"] >= 1
+
+
+@pytest.mark.parametrize("delta", [None, 50.0, 1000.0, 1e6])
+def test_grid_f32(delta, gb, orc):
+    a = gb.gen_grid(96, 128, 3, "f32")
+    run_and_check(gb, orc, a.row, a.col, a.w, 0, delta=delta)
+
+
+def test_f32_rmat_random_sources(gb, orc):
+    a = gb.gen_rmat(12, 16, 9, "f32")
+    for s in gb.sample_sources(a, 3, 2):
+        run_and_check(gb, orc, a.row, a.col, a.w, int(s))
+
+
+def test_isolated_source_and_unreached(gb, orc):
+    a = gb.gen_rmat(10, 4, 1)
+    deg = np.diff(a.row.astype(np.int64))
+    iso = int(np.nonzero(deg == 0)[0][0])
+    d, p, st = run_and_check(gb, orc, a.row, a.col, a.w, iso)
+    assert st["reached"] == 1 and d[iso] == 0 and p[iso] == iso
+    assert np.all(d[np.arange(a.n) != iso] == U32MAX) and np.all(p[np.arange(a.n) != iso] == -1)
+
+
+def test_multi_source_rows_match_single(gb, orc):
+    a = gb.gen_rmat(12, 16, 4)
+    srcs = gb.sample_sources(a, 4, 3)
+    with gb.Graph.from_host(a) as g:
+        D, P, st = g.sssp_multi(srcs, want_pred=True)
+        for i, s in enumerate(srcs):
+            d, p, _ = g.sssp(int(s))
+            assert np.array_equal(D[i], d) and np.array_equal(P[i], p)
+
+
+def test_device_outputs(gb, orc):
+    """gbs_sssp_device writes into caller-owned device memory (torch tensors
+    here, used only as device allocations)."""
+    torch = pytest.importorskip("torch")
+    a = gb.gen_rmat(11, 16, 6)
+    dd = torch.empty(a.n, dtype=torch.int32, device="cuda")
+    pd = torch.empty(a.n, dtype=torch.int32, device="cuda")
+    with gb.Graph.from_host(a) as g:
+        g.sssp_device(5, dd.data_ptr(), pd.data_ptr())
+        d, p, _ = g.sssp(5)
+    assert np.array_equal(dd.cpu().numpy().view(np.uint32), d)
+    assert np.array_equal(pd.cpu().numpy(), p)
+
+
+def test_invalid_source(gb):
+    a = gb.gen_rmat(8, 4, 1)
+    with gb.Graph.from_host(a) as g:
+        with pytest.raises(gb.GbsError) as e:
+            g.sssp(a.n)
+        assert e.value.name == "INVALID_ARG"
+
+
+def test_wait_limit_returns_timeout_and_device_recovers(gb, orc):
+    """One CTA never arrives at the first barrier (GBS_F_TEST_STALL): every
+    bounded wait runs out, the call reports TIMEOUT, and the next run on the
+    same graph is correct."""
+    a = gb.gen_rmat(10, 16, 2)
+    with gb.Graph.from_host(a) as g:
+        with pytest.raises(gb.GbsError) as e:
+            g.sssp(3, flags=0x80000000, wait_limit_ms=200)
+        assert e.value.name == "TIMEOUT"
+        d, p, _ = g.sssp(3)
+    ref = orc.dijkstra(a.row, a.col, a.w, 3)
+    assert np.array_equal(d, ref)
+
+
+def test_reference_mirror_run_sspath_arr(gb, orc):
+    """The Python mirror of run_sspath_arr over a t_csr-shaped CSR (inclusive
+    int64 end offsets, double weights) returns the reference's doubles."""
+    a = gb.gen_rmat(11, 16, 8)
+    gs = gb.TCsr(a.row[1:].astype(np.int64), a.col.astype(np.int64), a.w.astype(np.float64))
+    out = gb.run_sspath_arr(gs, 17, 9.0)
+    ref = orc.dijkstra(a.row, a.col, a.w, 17).astype(np.float64)
+    ref[ref == U32MAX] = np.inf
+    assert np.array_equal(out, ref) and np.array_equal(gs.weight, ref)
