@@ -293,7 +293,7 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": algo_bytes / K,
                          "traffic": traffic.get("bytes_per_launch") if traffic else None,
                          "traffic_source": traffic.get("source") if traffic else None},
-            "e2e": {"value": e2e_edges_all / e2e_max / 1e9, "unit": "GTEPS",
+            "e2e": {"value": e2e_edges_all / e2e_max / 1e9 if e2e_max > 0 else None, "unit": "GTEPS",
                     "h2d_bytes_per_step": 4,
                     "d2h_bytes_per_step": hg.n * 8 + 1024,
                     "steps": ke,

@@ -34,7 +34,7 @@ F_NO_STATS = 0x1
 EXPORTS = [
     "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
-    "gbs_sssp_multi", "gbs_host_alloc", "gbs_host_free", "gbs_device_alloc", "gbs_device_free",
+    "gbs_sssp_multi", "gbs_trace", "gbs_host_alloc", "gbs_host_free", "gbs_device_alloc", "gbs_device_free",
     "gbs_device_synchronize",
     "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
 ]
@@ -50,7 +50,17 @@ class GbsError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
                 ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
-                ("big_threshold", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("reserved", ctypes.c_uint32 * 2)]
+
+
+class PhaseRec(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("bucket", ctypes.c_uint32), ("items", ctypes.c_uint32),
+                ("edges", ctypes.c_uint32), ("end_ns", ctypes.c_uint64)]
+
+
+PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "scan_heavy", 3: "relax", 4: "pending"}
+F_TRACE = 0x2
+F_TEST_STALL = 0x80000000
 
 
 class Stats(ctypes.Structure):
@@ -98,6 +108,7 @@ def _load() -> ctypes.CDLL:
                                ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.POINTER(HostCsr))]
     L.gbs_sample_sources.argtypes = [ctypes.POINTER(HostCsr), ctypes.c_uint32, ctypes.c_uint64, P, P]
     L.gbs_host_csr_free.argtypes = [ctypes.POINTER(HostCsr)]
+    L.gbs_trace.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
     return L
 
 
@@ -287,9 +298,22 @@ class Graph:
 
     @staticmethod
     def params(delta: float | None = None, light: float | None = None, flags: int = 0,
-               wait_limit_ms: int = 0, big_threshold: int = 0) -> Params:
-        return Params(float(delta) if delta else 0.0, float(light) if light is not None else -1.0,
-                      flags, wait_limit_ms, big_threshold, 0)
+               wait_limit_ms: int = 0) -> Params:
+        p = Params()
+        p.delta = float(delta) if delta else 0.0
+        p.light = float(light) if light is not None else -1.0
+        p.flags = flags
+        p.wait_limit_ms = wait_limit_ms
+        return p
+
+    def trace(self) -> list[dict]:
+        """Per-phase records of the last run made with flags=F_TRACE."""
+        cnt = ctypes.c_uint32()
+        _check(lib.gbs_trace(self._h, None, 0, ctypes.byref(cnt)), "gbs_trace")
+        recs = (PhaseRec * max(1, cnt.value))()
+        _check(lib.gbs_trace(self._h, recs, cnt.value, ctypes.byref(cnt)), "gbs_trace")
+        return [{"kind": PHASE_KINDS.get(r.kind, r.kind), "bucket": r.bucket, "items": r.items,
+                 "edges": r.edges, "end_ns": r.end_ns} for r in recs[: cnt.value]]
 
     def sssp(self, source: int, delta: float | None = None, light: float | None = None,
              out_dist: np.ndarray | None = None, out_pred: np.ndarray | None = None,

@@ -120,6 +120,7 @@ struct gbs_graph {
     uint32_t mid_light_bits = 0;
     bool mid_valid = false;
     uint32_t epoch = 1, hround = 1;
+    uint32_t trace_n = 0;
     int blocks = 0;
     Ctl host_ctl{};
 };
@@ -166,11 +167,13 @@ gbs_status ensure_workspace(gbs_graph *g) {
     GBS_CUDA(cudaMalloc(&w.fq, sizeof(uint32_t) * n * 3));
     GBS_CUDA(cudaMalloc(&w.S, sizeof(uint32_t) * n * 2));
     GBS_CUDA(cudaMalloc(&w.pend, sizeof(uint32_t) * n * 2));
-    // one frontier holds each vertex at most once, so one phase pushes at most
-    // sum(len/kChunk + 1) <= 2m/kChunk chunks (rows split only if len >= kChunk)
-    const uint64_t cap = 2 * g->m / kChunk + 64;
-    w.big_cap = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFF0ull);
-    GBS_CUDA(cudaMalloc(&w.big, sizeof(uint4) * (size_t)w.big_cap * 2));
+    // a SCAN reads at most n entries and cuts each row into ceil(len/kDescEdges)
+    // descriptors, so it emits at most n + m/kDescEdges of them
+    const uint64_t cap = (uint64_t)g->n + g->m / kDescEdges + 64;
+    w.desc_cap = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFF0ull);
+    GBS_CUDA(cudaMalloc(&w.desc, sizeof(uint4) * (size_t)w.desc_cap));
+    w.trace = nullptr;
+    w.trace_cap = 0;
     GBS_CUDA(cudaMalloc(&w.ctl, sizeof(Ctl)));
     GBS_CUDA(cudaMalloc(&g->d_dist, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&g->d_pred, sizeof(int32_t) * n));
@@ -194,7 +197,8 @@ void free_graph(gbs_graph *g) {
     cudaFree(g->d_adj);
     Workspace &w = g->ws;
     cudaFree(w.dp); cudaFree(w.tag); cudaFree(w.fst); cudaFree(w.hst); cudaFree(w.mid);
-    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.big); cudaFree(w.ctl);
+    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.desc); cudaFree(w.ctl);
+    cudaFree(w.trace);
     cudaFree(g->d_dist);
     cudaFree(g->d_pred);
     for (auto &e : g->ev) if (e) cudaEventDestroy(e);
@@ -278,7 +282,13 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.hround0 = g->hround;
     a.delta_u = r.delta_u;
     a.inv_delta_f = r.inv_delta_f;
-    a.big_threshold = (p && p->big_threshold) ? std::max<uint32_t>(p->big_threshold, kChunk) : 2048u;
+    if (a.flags & GBS_F_TRACE) {
+        if (!g->ws.trace) {
+            g->ws.trace_cap = 1u << 20;
+            GBS_CUDA(cudaMalloc(&g->ws.trace, sizeof(TraceRec) * g->ws.trace_cap));
+        }
+        a.ws = g->ws;
+    }
     a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
     a.flags = p ? p->flags : 0u;
     a.run_ns = a.wait_ns * 16ull;
@@ -309,8 +319,9 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     GBS_CUDA(cudaMemcpyAsync(&g->host_ctl, g->ws.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     GBS_CUDA(cudaStreamSynchronize(s));
     const Ctl &c = g->host_ctl;
-    g->epoch = c.err_info + 1;
-    g->hround = c.pad4 + 1;
+    g->epoch = c.next_epoch + 1;
+    g->hround = c.next_hround + 1;
+    g->trace_n = (a.flags & GBS_F_TRACE) ? std::min(c.trace_n, g->ws.trace_cap) : 0u;
     if (c.error != kErrNone) {
         // stamps of an aborted run are unknown: start over next time
         g->epoch = 0xF0000001u;
@@ -510,6 +521,16 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k, con
         total.light_used = one.light_used;
     }
     if (stats) *stats = total;
+    return GBS_OK;
+}
+
+gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *count) {
+    if (!g || !count) return fail(GBS_ERR_INVALID_ARG, "NULL argument");
+    static_assert(sizeof(gbs_phase_rec) == sizeof(TraceRec), "trace record layout");
+    *count = g->trace_n;
+    const uint32_t k = std::min(cap, g->trace_n);
+    if (k && out)
+        GBS_CUDA(cudaMemcpy(out, g->ws.trace, sizeof(TraceRec) * k, cudaMemcpyDeviceToHost));
     return GBS_OK;
 }
 

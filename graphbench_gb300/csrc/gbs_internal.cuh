@@ -14,12 +14,12 @@
 //   tag[n]    uint32  smallest bucket the vertex was queued for (ring dedup)
 //   fst[n]    uint32  frontier stamp (dedup inside one light sub-phase)
 //   hst[n]    uint32  heavy-round stamp (dedup of the settled list S)
-//   ring      NB lists of n uint32: bucket b lives in list b % NB while it is
-//                     inside the window [W, W + NB)
-//   fq        3 lists of n uint32: current-bucket frontier, rotated per phase
+//   ring      kNB lists of n uint32: bucket b lives in list b % kNB while it is
+//                     inside the window [W, W + kNB)
+//   fq        3 lists of n uint32: current-bucket frontier, rotated per step
 //   S         2 lists of n uint32: vertices settled in the current bucket
 //   pend      2 lists of n uint32: vertices whose bucket is beyond the window
-//   big       2 lists of chunk descriptors for very long edge lists
+//   desc      edge descriptors {u, dist(u), first edge, end edge} of one SCAN
 #pragma once
 
 #include <cstdint>
@@ -34,8 +34,7 @@ constexpr uint32_t kTagInit = 0xFFFFFFFFu;
 constexpr uint32_t kTagPending = 0xFFFFFFFEu;
 constexpr uint32_t kBucketMax = 0xFFFFFF00u;
 constexpr unsigned long long kUnreached = ~0ull;
-constexpr uint32_t kChunk = 512;        // edges per big-list chunk
-constexpr int kTPB = 512;               // threads per CTA of the persistent kernel
+constexpr int kTPB = 1024;              // threads per CTA of the persistent kernel
 
 enum ErrCode : uint32_t {
     kErrNone = 0,
@@ -44,31 +43,41 @@ enum ErrCode : uint32_t {
     kErrOverflow = 3,
 };
 
-enum Mode : uint32_t { kModeBucket = 0, kModePending = 1, kModeDone = 2 };
+// One record per grid phase when GBS_F_TRACE is set (layout = gbs_phase_rec).
+struct TraceRec {
+    uint32_t kind;
+    uint32_t bucket;
+    uint32_t items;
+    uint32_t edges;
+    unsigned long long end_ns;
+};
 
 // Control block in global memory.  Barrier words sit on their own 128-byte
-// lines; the rest is read by every CTA after each barrier.
+// lines; the rest is read by the deciding CTA after each phase.
 struct __align__(128) Ctl {
     uint32_t bar_count;
     uint32_t pad0[31];
     uint32_t bar_gen;
     uint32_t pad1[31];
     uint32_t error;
-    uint32_t err_info;
     uint32_t mode;          // decision published by the last CTA at a barrier
     uint32_t next_bucket;
+    uint32_t trace_n;
     uint32_t pad2[28];
     uint32_t ring_cnt[kNB];
     uint32_t fq_cnt[3];
     uint32_t s_cnt[2];
     uint32_t pend_cnt[2];
     uint32_t pend_min[2];
-    uint32_t big_cnt[2];
+    uint32_t desc_cnt;
+    uint32_t edge_cnt;
     uint32_t pad3[21];
-    // statistics (written by CTA 0 at exit)
+    // statistics and carried state (written by CTA 0 at exit)
     uint32_t st_buckets;
     uint32_t st_phases;
     uint32_t st_pending_scans;
+    uint32_t next_epoch;
+    uint32_t next_hround;
     uint32_t pad4;
     unsigned long long st_improvements;
     unsigned long long st_reached;
@@ -87,8 +96,10 @@ struct Workspace {
     unsigned long long *dp;
     uint32_t *tag, *fst, *hst, *mid;
     uint32_t *ring, *fq, *S, *pend;
-    uint4 *big;
-    uint32_t big_cap;
+    uint4 *desc;
+    uint32_t desc_cap;
+    TraceRec *trace;
+    uint32_t trace_cap;
     Ctl *ctl;
 };
 
@@ -101,7 +112,6 @@ struct SsspArgs {
     uint32_t hround0;       // first heavy-round stamp of this run
     uint32_t delta_u;       // uint32 bucket width (>= 1)
     float inv_delta_f;      // float32: bucket = floor(d * inv_delta)
-    uint32_t big_threshold;
     uint32_t flags;         // GBS_F_* of the call
     unsigned long long wait_ns;   // limit of one barrier wait
     unsigned long long run_ns;    // limit of the whole run
@@ -126,6 +136,7 @@ __device__ __forceinline__ unsigned long long globaltimer() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+// Edge stream: read once per relaxation, not worth keeping in L1.
 __device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
     uint2 v;
     asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];"

@@ -20,9 +20,15 @@
 //   is re-bucketed when the window reaches them.  Any relaxation order reaches
 //   the same least fixpoint because fl(d + w) is monotone in d, so the
 //   distances are bit-identical to Dijkstra's for every delta and split.
-// Edge lists are expanded per warp: short rows by a warp-wide prefix sum,
-// rows of 32+ edges by the whole warp, rows above big_threshold split into
-// 512-edge chunks that every warp of the GPU shares in an extra BIG phase.
+//
+// Each LIGHT/HEAVY step is two grid phases:
+//   SCAN   one thread per frontier entry: validate, read the row range, emit
+//          edge descriptors {u, dist(u), first, end} of at most kDescEdges
+//          edges (the reference's request list R, without materialising one
+//          triple per edge)
+//   EDGES  one warp per 32 descriptors, flattened by a warp prefix sum and
+//          relaxed kUnroll x 32 edges per round with all loads of a round in
+//          flight before any is used
 #pragma once
 
 #include "gbs_internal.cuh"
@@ -30,23 +36,25 @@
 namespace gbs {
 
 enum Phase : uint32_t {
-    kPhLightFirst = 0,
-    kPhLight = 1,
-    kPhHeavy = 2,
-    kPhBig = 3,
-    kPhPending = 4,
+    kPhLightFirst = 0,    // SCAN of the ring list of a new bucket
+    kPhLight = 1,         // SCAN of the next frontier of the same bucket
+    kPhHeavy = 2,         // SCAN of S for heavy edges
+    kPhEdges = 3,         // relax the descriptors of the preceding SCAN
+    kPhPending = 4,       // re-bucket the pending list
     kPhDone = 5,
 };
+
+constexpr int kUnroll = 4;
+constexpr uint32_t kDescEdges = 32u * kUnroll;   // edges per descriptor (one warp round)
 
 // Values identical in every CTA (the kernel's uniform state).
 struct Uniform {
     uint32_t phase;       // phase being executed
-    uint32_t logical;     // kPhLight or kPhHeavy: the phase a BIG step belongs to
+    uint32_t logical;     // kPhLight or kPhHeavy: the SCAN an EDGES phase belongs to
     uint32_t b;           // current bucket
     uint32_t W;           // ring window base
     uint32_t epoch;       // frontier stamp of the current frontier
     uint32_t hround;      // heavy-round stamp (selects the S list)
-    uint32_t big_sel;
     uint32_t pend_sel;
     uint32_t gen;         // barrier generation
     unsigned long long t0;  // globaltimer at kernel entry (per CTA)
@@ -119,55 +127,46 @@ __device__ __forceinline__ void warp_append(uint32_t *buf, uint32_t *cnt, uint32
     }
 }
 
-// Relaxes edge e of u (distance bits du).  Returns the queue id for the target.
+// Tentative distance of an edge (u32: overflow check; f32: one rounding).
 template <bool F32>
-__device__ __forceinline__ int relax_edge(const SsspArgs &a, const Targets &t, uint32_t e, uint32_t u,
-                                          uint32_t du, uint32_t &v_out, uint32_t &imp) {
-    const uint2 ew = ld_stream(a.g.adj + e);
-    const uint32_t v = ew.x;
-    uint32_t nd;
+__device__ __forceinline__ bool edge_sum(uint32_t du, uint32_t wbits, uint32_t &nd) {
     if (F32) {
-        nd = __float_as_uint(__fadd_rn(__uint_as_float(du), __uint_as_float(ew.y)));
-    } else {
-        const unsigned long long s = (unsigned long long)du + ew.y;
-        if (s >= 0xFFFFFFFFull) {
-            atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
-            return -1;
-        }
-        nd = (uint32_t)s;
+        nd = __float_as_uint(__fadd_rn(__uint_as_float(du), __uint_as_float(wbits)));
+        return true;
     }
-    const unsigned long long packed = ((unsigned long long)nd << 32) | u;
-    unsigned long long *dpv = a.ws.dp + v;
-    if (packed >= __ldcg(dpv)) return -1;
-    const unsigned long long old = atomicMin(dpv, packed);
-    if (packed >= old || nd >= (uint32_t)(old >> 32)) return -1;  // no distance decrease
-    ++imp;
-    v_out = v;
+    const unsigned long long s = (unsigned long long)du + wbits;
+    nd = (uint32_t)s;
+    return s < 0xFFFFFFFFull;
+}
+
+// The packed atomicMin lowered v's distance to nd: pick the list v joins.
+template <bool F32>
+__device__ __forceinline__ int classify_improved(const SsspArgs &a, const Targets &t, uint32_t v,
+                                                 uint32_t nd) {
     const uint32_t nb = bucket_of<F32>(nd, a);
     if (nb < t.cur_hi) {
         atomicMin(a.ws.tag + v, nb);
         return atomicExch(a.ws.fst + v, t.stamp_next) != t.stamp_next ? 0 : -1;
     }
-    if ((unsigned long long)nb < (unsigned long long)t.W + kNB) {
+    if ((unsigned long long)nb < (unsigned long long)t.W + kNB)
         return atomicMin(a.ws.tag + v, nb) > nb ? 1 + (int)(nb % kNB) : -1;
-    }
     atomicMin(&a.ws.ctl->pend_min[t.pend_sel], nb);
     return atomicMin(a.ws.tag + v, kTagPending) == kTagInit ? kNB + 1 : -1;
 }
 
-// Expands one frontier list.  vtag != kTagInit keeps only entries whose tag
-// equals it (ring slots may hold entries that moved to a lower bucket).
-template <bool F32>
-__device__ void expand_frontier(const SsspArgs &a, const Targets &t, const uint32_t *F, uint32_t count,
-                                uint32_t vtag, bool light, bool add_s, uint32_t hround,
-                                uint32_t big_sel, uint32_t &imp) {
+// ------------------------------------------------------------------- SCAN
+// One thread per frontier entry.  vtag != kTagInit keeps only entries whose
+// tag equals it (ring lists may hold entries that moved to a lower bucket).
+__device__ void scan_frontier(const SsspArgs &a, const uint32_t *F, uint32_t count, uint32_t vtag,
+                              bool light, bool add_s, uint32_t hround) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
-    const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
-    for (uint32_t base = warp_g * 32u; base < count; base += nwarps * 32u) {
+    uint32_t my_edges = 0;
+    for (uint32_t base = tid - lane; base < count; base += nthreads) {
         const uint32_t i = base + lane;
         uint32_t u = 0, du = 0, s = 0, e = 0;
         bool ok = false;
@@ -177,52 +176,58 @@ __device__ void expand_frontier(const SsspArgs &a, const Targets &t, const uint3
         }
         if (ok) {
             du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
-            const uint32_t r0 = __ldg(a.g.row + u);
-            const uint32_t r1 = __ldg(a.g.row + u + 1);
             const uint32_t md = __ldg(a.ws.mid + u);
-            s = light ? r0 : md;
-            e = light ? md : r1;
+            s = light ? __ldg(a.g.row + u) : md;
+            e = light ? md : __ldg(a.g.row + u + 1);
         }
         bool sflag = false;
         if (ok && add_s) sflag = atomicExch(a.ws.hst + u, hround) != hround;
         warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u], n, sflag, u, ctl);
+        // descriptors of <= kDescEdges edges, reserved with one atomic per warp
+        const uint32_t len = e - s;
+        const uint32_t nd = (len + kDescEdges - 1) / kDescEdges;
+        uint32_t incl = nd;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if (total == 0) continue;
+        uint32_t dbase = 0;
+        if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt, total);
+        dbase = __shfl_sync(FULL, dbase, 31);
+        const uint32_t pos = dbase + incl - nd;
+        if (pos + nd <= a.ws.desc_cap) {
+            for (uint32_t c = 0; c < nd; ++c) {
+                const uint32_t cs = s + c * kDescEdges;
+                a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
+            }
+        } else if (nd) {
+            atomicExch(&ctl->error, (uint32_t)kErrCapacity);
+        }
+        my_edges += len;
+    }
+    // edges handed to EDGES (statistics / trace)
+    for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
+    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt, my_edges);
+}
 
-        uint32_t len = e - s;
-        // very long rows -> shared chunk list (processed in the BIG phase)
-        if (len >= a.big_threshold) {
-            const uint32_t nch = (len + kChunk - 1) / kChunk;
-            const uint32_t pos = atomicAdd(&ctl->big_cnt[big_sel], nch);
-            if (pos + nch <= a.ws.big_cap) {
-                uint4 *dst = a.ws.big + (size_t)big_sel * a.ws.big_cap + pos;
-                for (uint32_t c = 0; c < nch; ++c) {
-                    const uint32_t cs = s + c * kChunk;
-                    const uint32_t ce = min(e, cs + kChunk);
-                    dst[c] = make_uint4(u, du, cs, ce);
-                }
-            } else {
-                atomicExch(&ctl->error, (uint32_t)kErrCapacity);
-            }
-            len = 0;
-        }
-        // rows of 32+ edges: the whole warp walks one row at a time
-        unsigned mm = __ballot_sync(FULL, len >= 32u);
-        if (len >= 32u) len = 0;
-        while (mm) {
-            const int l = __ffs(mm) - 1;
-            mm &= mm - 1;
-            const uint32_t su = __shfl_sync(FULL, s, l);
-            const uint32_t eu = __shfl_sync(FULL, e, l);
-            const uint32_t uu = __shfl_sync(FULL, u, l);
-            const uint32_t duu = __shfl_sync(FULL, du, l);
-            for (uint32_t j = su; j < eu; j += 32u) {
-                const uint32_t ej = j + lane;
-                int q = -1;
-                uint32_t v = 0;
-                if (ej < eu) q = relax_edge<F32>(a, t, ej, uu, duu, v, imp);
-                warp_enqueue(a, t, q, v);
-            }
-        }
-        // short rows: warp-wide prefix sum, 32 edges per step
+// ------------------------------------------------------------------ EDGES
+// One warp per group of 32 descriptors; the group's edges are flattened by a
+// warp prefix sum and relaxed kUnroll x 32 at a time.
+template <bool F32>
+__device__ void relax_edges(const SsspArgs &a, const Targets &t, uint32_t count, uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t groups = (count + 31u) / 32u;
+    for (uint32_t g = warp_g; g < groups; g += nwarps) {
+        const uint32_t idx = g * 32u + lane;
+        uint4 d = make_uint4(0, 0, 0, 0);
+        if (idx < count) d = __ldcg(a.ws.desc + idx);
+        const uint32_t len = d.w - d.z;
         uint32_t incl = len;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -231,42 +236,54 @@ __device__ void expand_frontier(const SsspArgs &a, const Targets &t, const uint3
         }
         const uint32_t total = __shfl_sync(FULL, incl, 31);
         const uint32_t excl = incl - len;
-        for (uint32_t k0 = 0; k0 < total; k0 += 32u) {
-            const uint32_t k = k0 + lane;
-            int owner = 0;
+        for (uint32_t k0 = 0; k0 < total; k0 += 32u * kUnroll) {
+            uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+            bool val[kUnroll];
 #pragma unroll
-            for (int step = 16; step >= 1; step >>= 1) {
-                const int cand = owner + step;
-                const uint32_t ex = __shfl_sync(FULL, excl, cand);
-                if (ex <= k) owner = cand;
+            for (int j = 0; j < kUnroll; ++j) {
+                const uint32_t k = k0 + 32u * j + lane;
+                int owner = 0;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int cand = owner + step;
+                    const uint32_t ex = __shfl_sync(FULL, excl, cand);
+                    if (ex <= k) owner = cand;
+                }
+                const uint32_t so = __shfl_sync(FULL, d.z, owner);
+                const uint32_t exo = __shfl_sync(FULL, excl, owner);
+                uo[j] = __shfl_sync(FULL, d.x, owner);
+                duo[j] = __shfl_sync(FULL, d.y, owner);
+                val[j] = k < total;
+                v[j] = 0;
+                w[j] = 0;
+                if (val[j]) {
+                    const uint2 ew = ld_stream(a.g.adj + so + (k - exo));
+                    v[j] = ew.x;
+                    w[j] = ew.y;
+                }
             }
-            const uint32_t so = __shfl_sync(FULL, s, owner);
-            const uint32_t exo = __shfl_sync(FULL, excl, owner);
-            const uint32_t uo = __shfl_sync(FULL, u, owner);
-            const uint32_t duo = __shfl_sync(FULL, du, owner);
-            int q = -1;
-            uint32_t v = 0;
-            if (k < total) q = relax_edge<F32>(a, t, so + (k - exo), uo, duo, v, imp);
-            warp_enqueue(a, t, q, v);
-        }
-    }
-}
-
-template <bool F32>
-__device__ void expand_big(const SsspArgs &a, const Targets &t, uint32_t big_sel, uint32_t count,
-                           uint32_t &imp) {
-    const unsigned lane = lane_id();
-    const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint4 *list = a.ws.big + (size_t)big_sel * a.ws.big_cap;
-    for (uint32_t c = warp_g; c < count; c += nwarps) {
-        const uint4 ch = __ldcg(list + c);
-        for (uint32_t j = ch.z; j < ch.w; j += 32u) {
-            const uint32_t ej = j + lane;
-            int q = -1;
-            uint32_t v = 0;
-            if (ej < ch.w) q = relax_edge<F32>(a, t, ej, ch.x, ch.y, v, imp);
-            warp_enqueue(a, t, q, v);
+            unsigned long long cur[kUnroll];
+#pragma unroll
+            for (int j = 0; j < kUnroll; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
+            int q[kUnroll];
+#pragma unroll
+            for (int j = 0; j < kUnroll; ++j) {
+                q[j] = -1;
+                uint32_t nd;
+                if (!val[j]) continue;
+                if (!edge_sum<F32>(duo[j], w[j], nd)) {
+                    atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
+                    continue;
+                }
+                const unsigned long long packed = ((unsigned long long)nd << 32) | uo[j];
+                if (packed >= cur[j]) continue;
+                const unsigned long long old = atomicMin(a.ws.dp + v[j], packed);
+                if (packed >= old || nd >= (uint32_t)(old >> 32)) continue;  // no distance decrease
+                ++imp;
+                q[j] = classify_improved<F32>(a, t, v[j], nd);
+            }
+#pragma unroll
+            for (int j = 0; j < kUnroll; ++j) warp_enqueue(a, t, q[j], v[j]);
         }
     }
 }
@@ -308,6 +325,10 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U) {
     }
 }
 
+__device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
+    return phase == kPhHeavy ? (uint32_t)kPhHeavy : (uint32_t)kPhLight;
+}
+
 // Run by warp 0 of the CTA that arrives last at a barrier: every other CTA
 // has finished the phase, so all counters are at rest.  Decides the next
 // phase, resets the lists that phase will append to, and publishes.
@@ -315,9 +336,18 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
+    // one round trip: lanes 0..kNB-1 of two passes read the ring counters,
+    // lane 0 the other counters
+    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane]);
+    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32]);
+    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt);
+    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u]);
+    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0]), pc1 = ld_relaxed(&ctl->pend_cnt[1]);
+    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0]), pm1 = ld_relaxed(&ctl->pend_min[1]);
+    const uint32_t err = ld_relaxed(&ctl->error);
+
     uint32_t next = kPhDone, nb = 0;
-    // state after the update every CTA applies (mirrors advance_uniform)
-    uint32_t e2 = U.epoch, h2 = U.hround, bs2 = U.big_sel, ps2 = U.pend_sel;
+    uint32_t e2 = U.epoch, h2 = U.hround, ps2 = U.pend_sel;
     bool need_ring_scan = false;
     uint32_t scan_from = 0;
     if (U.phase == kPhPending) {
@@ -325,23 +355,20 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
         need_ring_scan = true;
         scan_from = U.W;
         if (lane == 0) { ctl->pend_cnt[U.pend_sel] = 0; ctl->pend_min[U.pend_sel] = kTagInit; }
+    } else if (U.phase != kPhEdges && desc_cnt > 0) {
+        next = kPhEdges;
     } else {
-        const uint32_t logical = (U.phase == kPhBig) ? U.logical : (U.phase == kPhHeavy ? kPhHeavy : kPhLight);
-        if (U.phase != kPhBig && ld_relaxed(&ctl->big_cnt[U.big_sel]) > 0) {
-            next = kPhBig;
+        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
+        e2 = U.epoch + 1;
+        if (logical == kPhHeavy) h2 = U.hround + 1;
+        if (fq_next > 0) {
+            next = kPhLight;
+        } else if (logical == kPhLight) {
+            next = kPhHeavy;
         } else {
-            e2 = U.epoch + 1;
-            bs2 = U.big_sel ^ 1u;
-            if (logical == kPhHeavy) h2 = U.hround + 1;
-            if (ld_relaxed(&ctl->fq_cnt[e2 % 3u]) > 0) {
-                next = kPhLight;
-            } else if (logical == kPhLight) {
-                next = kPhHeavy;
-            } else {
-                if (lane == 0) ctl->ring_cnt[U.b % kNB] = 0;
-                need_ring_scan = true;
-                scan_from = U.b + 1;
-            }
+            if (lane == 0) ctl->ring_cnt[U.b % kNB] = 0;
+            need_ring_scan = true;
+            scan_from = U.b + 1;
         }
     }
     if (need_ring_scan) {
@@ -349,14 +376,18 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
         // scan_from = b + 1 = W + 1, so the slot just cleared is not read.
         const uint32_t lim = U.W + kNB;   // exclusive
         uint32_t found = 0xFFFFFFFFu;
+#pragma unroll
         for (uint32_t off = 0; off < (uint32_t)kNB; off += 32u) {
             const uint32_t bk = scan_from + off + lane;
-            const bool nz = bk < lim && ld_relaxed(&ctl->ring_cnt[bk % kNB]) > 0;
-            const unsigned m = __ballot_sync(FULL, nz);
+            const uint32_t slot = bk % kNB;
+            const uint32_t c_lo = __shfl_sync(FULL, ring_lo, slot & 31u);
+            const uint32_t c_hi = __shfl_sync(FULL, ring_hi, slot & 31u);
+            const uint32_t c = slot < 32 ? c_lo : c_hi;
+            const unsigned m = __ballot_sync(FULL, bk < lim && c > 0);
             if (m && found == 0xFFFFFFFFu) found = scan_from + off + (uint32_t)(__ffs(m) - 1);
         }
-        const uint32_t pcnt = ld_relaxed(&ctl->pend_cnt[ps2]);
-        const uint32_t pm = ld_relaxed(&ctl->pend_min[ps2]);
+        const uint32_t pcnt = ps2 ? pc1 : pc0;
+        const uint32_t pm = ps2 ? pm1 : pm0;
         if (pcnt > 0 && pm <= found) {
             next = kPhPending;
             nb = pm;
@@ -372,10 +403,33 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
         next = kPhDone;
         if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
     }
+    if (err) next = kPhDone;
     if (lane == 0) {
+        if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
+            const uint32_t ti = ctl->trace_n;
+            if (ti < a.ws.trace_cap) {
+                uint32_t items;
+                switch (U.phase) {
+                    case kPhLightFirst: items = ld_relaxed(&ctl->ring_cnt[U.b % kNB]); break;
+                    case kPhLight: items = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u]); break;
+                    case kPhHeavy: items = ld_relaxed(&ctl->s_cnt[U.hround & 1u]); break;
+                    case kPhEdges: items = desc_cnt; break;
+                    default: items = ld_relaxed(&ctl->pend_cnt[U.pend_sel]); break;
+                }
+                TraceRec r;
+                r.kind = U.phase;
+                r.bucket = U.b;
+                r.items = items;
+                r.edges = ld_relaxed(&ctl->edge_cnt);
+                r.end_ns = globaltimer() - U.t0;
+                a.ws.trace[ti] = r;
+            }
+            ctl->trace_n = ti + 1;
+        }
         if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
             ctl->fq_cnt[(e2 + 1u) % 3u] = 0;
-            ctl->big_cnt[bs2] = 0;
+            ctl->desc_cnt = 0;
+            ctl->edge_cnt = 0;
             if (h2 != U.hround || next == kPhLightFirst) ctl->s_cnt[h2 & 1u] = 0;
         }
         ctl->mode = next;
@@ -388,13 +442,12 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
 __device__ __forceinline__ void advance_uniform(Uniform &U, uint32_t next, uint32_t nb) {
     if (U.phase == kPhPending) {
         U.pend_sel ^= 1u;
-    } else if (next != kPhBig) {
-        const uint32_t logical = (U.phase == kPhBig) ? U.logical : (U.phase == kPhHeavy ? kPhHeavy : kPhLight);
-        U.epoch += 1;
-        U.big_sel ^= 1u;
-        if (logical == kPhHeavy) U.hround += 1;
+    } else if (next == kPhEdges) {
+        U.logical = scan_kind(U.phase);
     } else {
-        U.logical = (U.phase == kPhHeavy) ? kPhHeavy : kPhLight;
+        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
+        U.epoch += 1;
+        if (logical == kPhHeavy) U.hround += 1;
     }
     if (next == kPhLightFirst) { U.b = nb; U.W = nb; }
     if (next == kPhPending) U.W = nb;
@@ -446,7 +499,7 @@ __device__ __forceinline__ void grid_barrier(const SsspArgs &a, Uniform &U) {
 }
 
 template <bool F32>
-__global__ void __launch_bounds__(kTPB, 2) sssp_persistent(SsspArgs a) {
+__global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     Ctl *ctl = a.ws.ctl;
     Uniform U;
     U.phase = ld_relaxed(&ctl->mode);
@@ -455,12 +508,11 @@ __global__ void __launch_bounds__(kTPB, 2) sssp_persistent(SsspArgs a) {
     U.W = U.b;
     U.epoch = a.epoch0;
     U.hround = a.hround0;
-    U.big_sel = 0;
     U.pend_sel = 0;
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t imp = 0, nphases = 0, nbuckets = 0, nscans = 0;
-    const uint32_t ncap = a.g.n;   // every list holds at most n entries
+    const uint32_t ncap = a.g.n;   // every vertex list holds at most n entries
     __shared__ uint32_t s_next[2];
 
     while (U.phase != kPhDone) {
@@ -474,22 +526,19 @@ __global__ void __launch_bounds__(kTPB, 2) sssp_persistent(SsspArgs a) {
         switch (U.phase) {
             case kPhLightFirst:
                 ++nbuckets;
-                expand_frontier<F32>(a, t, a.ws.ring + (size_t)(U.b % kNB) * n,
-                                     min(__ldcg(&ctl->ring_cnt[U.b % kNB]), ncap), U.b, true, true,
-                                     U.hround, U.big_sel, imp);
+                scan_frontier(a, a.ws.ring + (size_t)(U.b % kNB) * n,
+                              min(__ldcg(&ctl->ring_cnt[U.b % kNB]), ncap), U.b, true, true, U.hround);
                 break;
             case kPhLight:
-                expand_frontier<F32>(a, t, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                                     min(__ldcg(&ctl->fq_cnt[U.epoch % 3u]), ncap), kTagInit, true, true,
-                                     U.hround, U.big_sel, imp);
+                scan_frontier(a, a.ws.fq + (size_t)(U.epoch % 3u) * n,
+                              min(__ldcg(&ctl->fq_cnt[U.epoch % 3u]), ncap), kTagInit, true, true, U.hround);
                 break;
             case kPhHeavy:
-                expand_frontier<F32>(a, t, a.ws.S + (size_t)(U.hround & 1u) * n,
-                                     min(__ldcg(&ctl->s_cnt[U.hround & 1u]), ncap), kTagInit, false, false,
-                                     U.hround, U.big_sel, imp);
+                scan_frontier(a, a.ws.S + (size_t)(U.hround & 1u) * n,
+                              min(__ldcg(&ctl->s_cnt[U.hround & 1u]), ncap), kTagInit, false, false, U.hround);
                 break;
-            case kPhBig:
-                expand_big<F32>(a, t, U.big_sel, min(__ldcg(&ctl->big_cnt[U.big_sel]), a.ws.big_cap), imp);
+            case kPhEdges:
+                relax_edges<F32>(a, t, min(__ldcg(&ctl->desc_cnt), a.ws.desc_cap), imp);
                 break;
             case kPhPending:
                 ++nscans;
@@ -516,8 +565,8 @@ __global__ void __launch_bounds__(kTPB, 2) sssp_persistent(SsspArgs a) {
         ctl->st_buckets = nbuckets;
         ctl->st_phases = nphases;
         ctl->st_pending_scans = nscans;
-        ctl->err_info = U.epoch;          // next free stamps for the following run
-        ctl->pad4 = U.hround;
+        ctl->next_epoch = U.epoch;        // next free stamps for the following run
+        ctl->next_hround = U.hround;
     }
 }
 

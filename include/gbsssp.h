@@ -66,13 +66,13 @@ typedef struct gbs_params {
                                 < 0 selects light = delta (the reference's rule,
                                 graph/csr.c:84). */
     uint32_t flags;          /* GBS_F_* */
-    uint32_t wait_limit_ms;  /* device-side wait limit; 0 = 4000 ms */
-    uint32_t big_threshold;  /* edges at or above which one vertex's edge list is
-                                split across the whole GPU; 0 = 2048 */
-    uint32_t reserved;
+    uint32_t wait_limit_ms;  /* device-side wait limit; 0 = 4000 ms (a whole run
+                                is limited to 16 times this) */
+    uint32_t reserved[2];
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
+#define GBS_F_TRACE 0x2u     /* record one gbs_phase_rec per grid phase (gbs_trace) */
 /* Failure-path test: one CTA never arrives at the first grid barrier, so every
  * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
  * wait_limit_ms and the device stays usable.  Never set in normal use. */
@@ -146,6 +146,26 @@ gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *para
 gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
                           const gbs_params *params, void *dist_out, int32_t *pred_out,
                           gbs_stats *stats);
+
+/*
+ * Per-phase record of the last run made with GBS_F_TRACE (the GPU analogue
+ * of the reference's per-phase rdtsc slots and bucket dumps,
+ * sssp/csr_sspath_array.c:1121-1170).  kind: 0 scan of a new bucket, 1 scan
+ * of a repeated light frontier, 2 scan of the settled list for heavy edges,
+ * 3 edge relaxation, 4 pending re-bucketing.  items: frontier entries
+ * (scans), edge descriptors (relaxation) or pending entries; edges: edges
+ * the scan handed to the relaxation; end_ns: device time since kernel start.
+ * *count receives the number of records (may exceed cap).
+ */
+typedef struct gbs_phase_rec {
+    uint32_t kind;
+    uint32_t bucket;
+    uint32_t items;
+    uint32_t edges;
+    uint64_t end_ns;
+} gbs_phase_rec;
+
+gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *count);
 
 /* Pinned host memory for fast transfers. */
 gbs_status gbs_host_alloc(size_t bytes, void **out);

@@ -89,12 +89,34 @@ def test_rmat16_many_sources_one_graph(gb, orc):
             assert st["buckets"] >= 1 and st["phases"] >= 2
 
 
-def test_big_rows_split_across_gpu(gb, orc):
-    """A low big_threshold routes hub rows through the shared chunk list."""
+def test_hub_rows_split_into_descriptors(gb, orc):
+    """Hub rows (thousands of edges) are cut into 128-edge descriptors that
+    many warps relax; a huge delta puts every edge in the light part."""
     a = gb.gen_rmat(14, 32, 5)
+    assert np.diff(a.row.astype(np.int64)).max() > 1000
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
-    run_and_check(gb, orc, a.row, a.col, a.w, src, big_threshold=512)
-    run_and_check(gb, orc, a.row, a.col, a.w, src, big_threshold=512, delta=100000)
+    run_and_check(gb, orc, a.row, a.col, a.w, src)
+    run_and_check(gb, orc, a.row, a.col, a.w, src, delta=100000)
+
+
+def test_phase_trace(gb, orc):
+    """GBS_F_TRACE records one entry per grid phase; scans are followed by a
+    relaxation of the edges they emitted, and device time is monotone."""
+    a = gb.gen_rmat(12, 16, 2)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    with gb.Graph.from_host(a) as g:
+        d, _, st = g.sssp(src, flags=gb.F_TRACE)
+        tr = g.trace()
+        assert len(tr) == st["phases"]
+        assert sum(1 for r in tr if r["kind"] == "scan_bucket") == st["buckets"]
+        assert all(tr[i]["end_ns"] <= tr[i + 1]["end_ns"] for i in range(len(tr) - 1))
+        for i, r in enumerate(tr[:-1]):
+            if r["kind"].startswith("scan") and r["edges"] > 0:
+                assert tr[i + 1]["kind"] == "relax"
+                assert tr[i + 1]["edges"] == r["edges"]
+        # tracing changes nothing in the result
+        d2, _, _ = g.sssp(src)
+    assert np.array_equal(d, d2) and np.array_equal(d, orc.dijkstra(a.row, a.col, a.w, src))
 
 
 def test_pending_list_small_delta(gb, orc):
