@@ -282,6 +282,9 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.hround0 = g->hround;
     a.delta_u = r.delta_u;
     a.inv_delta_f = r.inv_delta_f;
+    a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
+    a.flags = p ? p->flags : 0u;
+    a.run_ns = a.wait_ns * 16ull;
     if (a.flags & GBS_F_TRACE) {
         if (!g->ws.trace) {
             g->ws.trace_cap = 1u << 20;
@@ -289,9 +292,6 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
         }
         a.ws = g->ws;
     }
-    a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
-    a.flags = p ? p->flags : 0u;
-    a.run_ns = a.wait_ns * 16ull;
 
     GBS_CUDA(cudaEventRecord(g->ev[0], s));
     GBS_CUDA(cudaMemsetAsync(g->ws.ctl, 0, sizeof(Ctl), s));
