@@ -60,9 +60,9 @@ __global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restric
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ring0[0] = src;
-        ctl->ring_cnt[0] = 1;
-        ctl->pend_min[0] = kTagInit;
-        ctl->pend_min[1] = kTagInit;
+        ctl->ring_cnt[0].v = 1;
+        ctl->pend_min[0].v = kTagInit;
+        ctl->pend_min[1].v = kTagInit;
         ctl->mode = kPhLightFirst;
         ctl->next_bucket = 0;
     }

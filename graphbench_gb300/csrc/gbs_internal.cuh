@@ -52,8 +52,16 @@ struct TraceRec {
     unsigned long long end_ns;
 };
 
-// Control block in global memory.  Barrier words sit on their own 128-byte
-// lines; the rest is read by the deciding CTA after each phase.
+// A counter alone on a 128-byte line: list counters take millions of
+// appends per run, and counters sharing a line serialise at one L2 slice.
+struct __align__(128) Line {
+    uint32_t v;
+    uint32_t pad[31];
+};
+
+// Control block in global memory.  Barrier words and every list counter sit
+// on their own 128-byte lines; the block is read by the deciding CTA after
+// each phase.
 struct __align__(128) Ctl {
     uint32_t bar_count;
     uint32_t pad0[31];
@@ -64,14 +72,13 @@ struct __align__(128) Ctl {
     uint32_t next_bucket;
     uint32_t trace_n;
     uint32_t pad2[28];
-    uint32_t ring_cnt[kNB];
-    uint32_t fq_cnt[3];
-    uint32_t s_cnt[2];
-    uint32_t pend_cnt[2];
-    uint32_t pend_min[2];
-    uint32_t desc_cnt;
-    uint32_t edge_cnt;
-    uint32_t pad3[21];
+    Line ring_cnt[kNB];
+    Line fq_cnt[3];
+    Line s_cnt[2];
+    Line pend_cnt[2];
+    Line pend_min[2];
+    Line desc_cnt;
+    Line edge_cnt;
     // statistics and carried state (written by CTA 0 at exit)
     uint32_t st_buckets;
     uint32_t st_phases;

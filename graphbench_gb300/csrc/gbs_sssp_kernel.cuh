@@ -21,14 +21,17 @@
 //   the same least fixpoint because fl(d + w) is monotone in d, so the
 //   distances are bit-identical to Dijkstra's for every delta and split.
 //
-// Each LIGHT/HEAVY step is two grid phases:
-//   SCAN   one thread per frontier entry: validate, read the row range, emit
-//          edge descriptors {u, dist(u), first, end} of at most kDescEdges
-//          edges (the reference's request list R, without materialising one
-//          triple per edge)
-//   EDGES  one warp per 32 descriptors, flattened by a warp prefix sum and
-//          relaxed kUnroll x 32 edges per round with all loads of a round in
-//          flight before any is used
+// Each LIGHT/HEAVY step is one or two grid phases:
+//   SCAN   one thread per frontier entry: validate and read the row range.
+//          Rows of at most kInlineEdges edges are relaxed right away by the
+//          scanning warp; longer rows become edge descriptors {u, dist(u),
+//          first, end} of at most kDescEdges edges (the reference's request
+//          list R, without one triple per edge).
+//   EDGES  only if descriptors exist: one warp per 32 descriptors.
+// Relaxation is warp-collective: the warp's edge ranges are flattened by a
+// prefix sum and relaxed kUnroll x 32 edges per round, with every load of a
+// round issued before any is used and one counter atomic per target list per
+// round.
 #pragma once
 
 #include "gbs_internal.cuh"
@@ -46,6 +49,7 @@ enum Phase : uint32_t {
 
 constexpr int kUnroll = 4;
 constexpr uint32_t kDescEdges = 32u * kUnroll;   // edges per descriptor (one warp round)
+constexpr uint32_t kInlineEdges = 32u;           // rows up to this long are relaxed in SCAN
 
 // Values identical in every CTA (the kernel's uniform state).
 struct Uniform {
@@ -81,31 +85,64 @@ struct Targets {
 };
 
 // Queue ids: -1 none, 0 next frontier, 1..kNB ring slots, kNB+1 pending.
-__device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t, int q, uint32_t v) {
-    const unsigned FULL = 0xffffffffu;
-    if (__ballot_sync(FULL, q >= 0) == 0) return;
-    const unsigned lane = lane_id();
-    const unsigned grp = __match_any_sync(FULL, q);
-    const int leader = __ffs(grp) - 1;
+__device__ __forceinline__ uint32_t *queue_counter(const SsspArgs &a, const Targets &t, int q) {
     Ctl *ctl = a.ws.ctl;
-    const uint32_t n = a.g.n;
-    uint32_t base = 0;
-    if (q >= 0 && (int)lane == leader) {
-        uint32_t *cnt;
-        if (q == 0) cnt = &ctl->fq_cnt[t.fq_next];
-        else if (q <= kNB) cnt = &ctl->ring_cnt[q - 1];
-        else cnt = &ctl->pend_cnt[t.pend_sel];
-        base = atomicAdd(cnt, (uint32_t)__popc(grp));
-    }
-    base = __shfl_sync(FULL, base, leader);
-    if (q >= 0) {
-        uint32_t pos = base + (uint32_t)__popc(grp & ((1u << lane) - 1u));
-        uint32_t *buf;
-        if (q == 0) buf = a.ws.fq + (size_t)t.fq_next * n;
-        else if (q <= kNB) buf = a.ws.ring + (size_t)(q - 1) * n;
-        else buf = a.ws.pend + (size_t)t.pend_sel * n;
-        if (pos < n) buf[pos] = v;
-        else atomicExch(&ctl->error, (uint32_t)kErrCapacity);
+    if (q == 0) return &ctl->fq_cnt[t.fq_next].v;
+    if (q <= kNB) return &ctl->ring_cnt[q - 1].v;
+    return &ctl->pend_cnt[t.pend_sel].v;
+}
+__device__ __forceinline__ uint32_t *queue_list(const SsspArgs &a, const Targets &t, int q) {
+    const size_t n = a.g.n;
+    if (q == 0) return a.ws.fq + (size_t)t.fq_next * n;
+    if (q <= kNB) return a.ws.ring + (size_t)(q - 1) * n;
+    return a.ws.pend + (size_t)t.pend_sel * n;
+}
+
+// Appends every (q[j], v[j]) with q[j] >= 0 of the whole warp: one pass per
+// distinct target list, one counter atomic per pass.
+template <int U>
+__device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t, const int (&q)[U],
+                                             const uint32_t (&v)[U]) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    unsigned pend = 0;
+#pragma unroll
+    for (int j = 0; j < U; ++j) pend |= (q[j] >= 0 ? 1u : 0u) << j;
+    for (;;) {
+        const unsigned any = __ballot_sync(FULL, pend != 0);
+        if (!any) break;
+        int myq = -1;
+#pragma unroll
+        for (int j = U - 1; j >= 0; --j)
+            if ((pend >> j) & 1u) myq = q[j];
+        const int Q = __shfl_sync(FULL, myq, __ffs(any) - 1);
+        unsigned mb = 0;
+#pragma unroll
+        for (int j = 0; j < U; ++j) mb |= (((pend >> j) & 1u) && q[j] == Q ? 1u : 0u) << j;
+        const uint32_t c = (uint32_t)__popc(mb);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        uint32_t base = 0;
+        if (lane == 31) base = atomicAdd(queue_counter(a, t, Q), total);
+        base = __shfl_sync(FULL, base, 31) + incl - c;
+        if (mb) {
+            uint32_t *buf = queue_list(a, t, Q);
+            const uint32_t n = a.g.n;
+#pragma unroll
+            for (int j = 0; j < U; ++j) {
+                if ((mb >> j) & 1u) {
+                    if (base < n) buf[base] = v[j];
+                    else atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
+                    ++base;
+                }
+            }
+        }
+        pend &= ~mb;
     }
 }
 
@@ -150,15 +187,81 @@ __device__ __forceinline__ int classify_improved(const SsspArgs &a, const Target
     }
     if ((unsigned long long)nb < (unsigned long long)t.W + kNB)
         return atomicMin(a.ws.tag + v, nb) > nb ? 1 + (int)(nb % kNB) : -1;
-    atomicMin(&a.ws.ctl->pend_min[t.pend_sel], nb);
+    atomicMin(&a.ws.ctl->pend_min[t.pend_sel].v, nb);
     return atomicMin(a.ws.tag + v, kTagPending) == kTagInit ? kNB + 1 : -1;
+}
+
+// Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
+// given by every lane (len may be 0), kUnroll x 32 edges per round.
+template <bool F32>
+__device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t, uint32_t u, uint32_t du,
+                                            uint32_t s, uint32_t len, uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if ((int)lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    const uint32_t excl = incl - len;
+    for (uint32_t k0 = 0; k0 < total; k0 += 32u * kUnroll) {
+        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+        bool val[kUnroll];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) {
+            const uint32_t k = k0 + 32u * j + lane;
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int cand = owner + step;
+                const uint32_t ex = __shfl_sync(FULL, excl, cand);
+                if (ex <= k) owner = cand;
+            }
+            const uint32_t so = __shfl_sync(FULL, s, owner);
+            const uint32_t exo = __shfl_sync(FULL, excl, owner);
+            uo[j] = __shfl_sync(FULL, u, owner);
+            duo[j] = __shfl_sync(FULL, du, owner);
+            val[j] = k < total;
+            v[j] = 0;
+            w[j] = 0;
+            if (val[j]) {
+                const uint2 ew = ld_stream(a.g.adj + so + (k - exo));
+                v[j] = ew.x;
+                w[j] = ew.y;
+            }
+        }
+        unsigned long long cur[kUnroll];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
+        int q[kUnroll];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) {
+            q[j] = -1;
+            uint32_t nd;
+            if (!val[j]) continue;
+            if (!edge_sum<F32>(duo[j], w[j], nd)) {
+                atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
+                continue;
+            }
+            const unsigned long long packed = ((unsigned long long)nd << 32) | uo[j];
+            if (packed >= cur[j]) continue;
+            const unsigned long long old = atomicMin(a.ws.dp + v[j], packed);
+            if (packed >= old || nd >= (uint32_t)(old >> 32)) continue;  // no distance decrease
+            ++imp;
+            q[j] = classify_improved<F32>(a, t, v[j], nd);
+        }
+        warp_enqueue<kUnroll>(a, t, q, v);
+    }
 }
 
 // ------------------------------------------------------------------- SCAN
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
-__device__ void scan_frontier(const SsspArgs &a, const uint32_t *F, uint32_t count, uint32_t vtag,
-                              bool light, bool add_s, uint32_t hround) {
+template <bool F32>
+__device__ void scan_frontier(const SsspArgs &a, const Targets &t, const uint32_t *F, uint32_t count,
+                              uint32_t vtag, bool light, bool add_s, uint32_t hround, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -182,10 +285,10 @@ __device__ void scan_frontier(const SsspArgs &a, const uint32_t *F, uint32_t cou
         }
         bool sflag = false;
         if (ok && add_s) sflag = atomicExch(a.ws.hst + u, hround) != hround;
-        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u], n, sflag, u, ctl);
-        // descriptors of <= kDescEdges edges, reserved with one atomic per warp
+        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n, sflag, u, ctl);
         const uint32_t len = e - s;
-        const uint32_t nd = (len + kDescEdges - 1) / kDescEdges;
+        // long rows -> descriptors, reserved with one atomic per warp
+        const uint32_t nd = len > kInlineEdges ? (len + kDescEdges - 1) / kDescEdges : 0u;
         uint32_t incl = nd;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -193,32 +296,32 @@ __device__ void scan_frontier(const SsspArgs &a, const uint32_t *F, uint32_t cou
             if ((int)lane >= o) incl += y;
         }
         const uint32_t total = __shfl_sync(FULL, incl, 31);
-        if (total == 0) continue;
-        uint32_t dbase = 0;
-        if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt, total);
-        dbase = __shfl_sync(FULL, dbase, 31);
-        const uint32_t pos = dbase + incl - nd;
-        if (pos + nd <= a.ws.desc_cap) {
-            for (uint32_t c = 0; c < nd; ++c) {
-                const uint32_t cs = s + c * kDescEdges;
-                a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
+        if (total) {
+            uint32_t dbase = 0;
+            if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt.v, total);
+            dbase = __shfl_sync(FULL, dbase, 31);
+            const uint32_t pos = dbase + incl - nd;
+            if (pos + nd <= a.ws.desc_cap) {
+                for (uint32_t c = 0; c < nd; ++c) {
+                    const uint32_t cs = s + c * kDescEdges;
+                    a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
+                }
+            } else if (nd) {
+                atomicExch(&ctl->error, (uint32_t)kErrCapacity);
             }
-        } else if (nd) {
-            atomicExch(&ctl->error, (uint32_t)kErrCapacity);
+            my_edges += nd ? len : 0u;
         }
-        my_edges += len;
+        // short rows: relaxed by this warp now
+        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, imp);
     }
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
-    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt, my_edges);
+    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
 }
 
 // ------------------------------------------------------------------ EDGES
-// One warp per group of 32 descriptors; the group's edges are flattened by a
-// warp prefix sum and relaxed kUnroll x 32 at a time.
 template <bool F32>
-__device__ void relax_edges(const SsspArgs &a, const Targets &t, uint32_t count, uint32_t &imp) {
-    const unsigned FULL = 0xffffffffu;
+__device__ void relax_descriptors(const SsspArgs &a, const Targets &t, uint32_t count, uint32_t &imp) {
     const unsigned lane = lane_id();
     const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -227,64 +330,7 @@ __device__ void relax_edges(const SsspArgs &a, const Targets &t, uint32_t count,
         const uint32_t idx = g * 32u + lane;
         uint4 d = make_uint4(0, 0, 0, 0);
         if (idx < count) d = __ldcg(a.ws.desc + idx);
-        const uint32_t len = d.w - d.z;
-        uint32_t incl = len;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, o);
-            if ((int)lane >= o) incl += y;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        const uint32_t excl = incl - len;
-        for (uint32_t k0 = 0; k0 < total; k0 += 32u * kUnroll) {
-            uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
-            bool val[kUnroll];
-#pragma unroll
-            for (int j = 0; j < kUnroll; ++j) {
-                const uint32_t k = k0 + 32u * j + lane;
-                int owner = 0;
-#pragma unroll
-                for (int step = 16; step >= 1; step >>= 1) {
-                    const int cand = owner + step;
-                    const uint32_t ex = __shfl_sync(FULL, excl, cand);
-                    if (ex <= k) owner = cand;
-                }
-                const uint32_t so = __shfl_sync(FULL, d.z, owner);
-                const uint32_t exo = __shfl_sync(FULL, excl, owner);
-                uo[j] = __shfl_sync(FULL, d.x, owner);
-                duo[j] = __shfl_sync(FULL, d.y, owner);
-                val[j] = k < total;
-                v[j] = 0;
-                w[j] = 0;
-                if (val[j]) {
-                    const uint2 ew = ld_stream(a.g.adj + so + (k - exo));
-                    v[j] = ew.x;
-                    w[j] = ew.y;
-                }
-            }
-            unsigned long long cur[kUnroll];
-#pragma unroll
-            for (int j = 0; j < kUnroll; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
-            int q[kUnroll];
-#pragma unroll
-            for (int j = 0; j < kUnroll; ++j) {
-                q[j] = -1;
-                uint32_t nd;
-                if (!val[j]) continue;
-                if (!edge_sum<F32>(duo[j], w[j], nd)) {
-                    atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
-                    continue;
-                }
-                const unsigned long long packed = ((unsigned long long)nd << 32) | uo[j];
-                if (packed >= cur[j]) continue;
-                const unsigned long long old = atomicMin(a.ws.dp + v[j], packed);
-                if (packed >= old || nd >= (uint32_t)(old >> 32)) continue;  // no distance decrease
-                ++imp;
-                q[j] = classify_improved<F32>(a, t, v[j], nd);
-            }
-#pragma unroll
-            for (int j = 0; j < kUnroll; ++j) warp_enqueue(a, t, q[j], v[j]);
-        }
+        relax_group<F32>(a, t, d.x, d.y, d.z, d.w - d.z, imp);
     }
 }
 
@@ -294,7 +340,7 @@ template <bool F32>
 __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U) {
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
-    const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel]), n);
+    const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
     const uint32_t *list = a.ws.pend + (size_t)U.pend_sel * n;
     Targets t;
     t.cur_hi = 0;
@@ -306,22 +352,22 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U) {
     const uint32_t nthreads = gridDim.x * blockDim.x;
     for (uint32_t base = tid - lane_id(); base < count; base += nthreads) {
         const uint32_t i = base + lane_id();
-        int q = -1;
-        uint32_t v = 0;
+        int q[1] = {-1};
+        uint32_t v[1] = {0};
         if (i < count) {
-            v = __ldcg(list + i);
-            if (__ldcg(a.ws.tag + v) == kTagPending) {
-                const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v) >> 32), a);
+            v[0] = __ldcg(list + i);
+            if (__ldcg(a.ws.tag + v[0]) == kTagPending) {
+                const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v[0]) >> 32), a);
                 if ((unsigned long long)nb < (unsigned long long)U.W + kNB) {
-                    a.ws.tag[v] = nb;
-                    q = 1 + (int)(nb % kNB);
+                    a.ws.tag[v[0]] = nb;
+                    q[0] = 1 + (int)(nb % kNB);
                 } else {
-                    atomicMin(&ctl->pend_min[t.pend_sel], nb);
-                    q = kNB + 1;
+                    atomicMin(&ctl->pend_min[t.pend_sel].v, nb);
+                    q[0] = kNB + 1;
                 }
             }
         }
-        warp_enqueue(a, t, q, v);
+        warp_enqueue<1>(a, t, q, v);
     }
 }
 
@@ -336,14 +382,13 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
-    // one round trip: lanes 0..kNB-1 of two passes read the ring counters,
-    // lane 0 the other counters
-    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane]);
-    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32]);
-    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt);
-    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u]);
-    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0]), pc1 = ld_relaxed(&ctl->pend_cnt[1]);
-    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0]), pm1 = ld_relaxed(&ctl->pend_min[1]);
+    // one round trip: every counter the decision needs is loaded at once
+    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane].v);
+    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32].v);
+    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt.v);
+    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u].v);
+    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0].v), pc1 = ld_relaxed(&ctl->pend_cnt[1].v);
+    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0].v), pm1 = ld_relaxed(&ctl->pend_min[1].v);
     const uint32_t err = ld_relaxed(&ctl->error);
 
     uint32_t next = kPhDone, nb = 0;
@@ -354,7 +399,7 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
         ps2 ^= 1u;
         need_ring_scan = true;
         scan_from = U.W;
-        if (lane == 0) { ctl->pend_cnt[U.pend_sel] = 0; ctl->pend_min[U.pend_sel] = kTagInit; }
+        if (lane == 0) { ctl->pend_cnt[U.pend_sel].v = 0; ctl->pend_min[U.pend_sel].v = kTagInit; }
     } else if (U.phase != kPhEdges && desc_cnt > 0) {
         next = kPhEdges;
     } else {
@@ -366,7 +411,7 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
         } else if (logical == kPhLight) {
             next = kPhHeavy;
         } else {
-            if (lane == 0) ctl->ring_cnt[U.b % kNB] = 0;
+            if (lane == 0) ctl->ring_cnt[U.b % kNB].v = 0;
             need_ring_scan = true;
             scan_from = U.b + 1;
         }
@@ -410,27 +455,27 @@ __device__ void control_step(const SsspArgs &a, const Uniform &U) {
             if (ti < a.ws.trace_cap) {
                 uint32_t items;
                 switch (U.phase) {
-                    case kPhLightFirst: items = ld_relaxed(&ctl->ring_cnt[U.b % kNB]); break;
-                    case kPhLight: items = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u]); break;
-                    case kPhHeavy: items = ld_relaxed(&ctl->s_cnt[U.hround & 1u]); break;
+                    case kPhLightFirst: items = ld_relaxed(&ctl->ring_cnt[U.b % kNB].v); break;
+                    case kPhLight: items = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u].v); break;
+                    case kPhHeavy: items = ld_relaxed(&ctl->s_cnt[U.hround & 1u].v); break;
                     case kPhEdges: items = desc_cnt; break;
-                    default: items = ld_relaxed(&ctl->pend_cnt[U.pend_sel]); break;
+                    default: items = ld_relaxed(&ctl->pend_cnt[U.pend_sel].v); break;
                 }
                 TraceRec r;
                 r.kind = U.phase;
                 r.bucket = U.b;
                 r.items = items;
-                r.edges = ld_relaxed(&ctl->edge_cnt);
+                r.edges = ld_relaxed(&ctl->edge_cnt.v);
                 r.end_ns = globaltimer() - U.t0;
                 a.ws.trace[ti] = r;
             }
             ctl->trace_n = ti + 1;
         }
         if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
-            ctl->fq_cnt[(e2 + 1u) % 3u] = 0;
-            ctl->desc_cnt = 0;
-            ctl->edge_cnt = 0;
-            if (h2 != U.hround || next == kPhLightFirst) ctl->s_cnt[h2 & 1u] = 0;
+            ctl->fq_cnt[(e2 + 1u) % 3u].v = 0;
+            ctl->desc_cnt.v = 0;
+            ctl->edge_cnt.v = 0;
+            if (h2 != U.hround || next == kPhLightFirst) ctl->s_cnt[h2 & 1u].v = 0;
         }
         ctl->mode = next;
         ctl->next_bucket = nb;
@@ -526,19 +571,22 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
         switch (U.phase) {
             case kPhLightFirst:
                 ++nbuckets;
-                scan_frontier(a, a.ws.ring + (size_t)(U.b % kNB) * n,
-                              min(__ldcg(&ctl->ring_cnt[U.b % kNB]), ncap), U.b, true, true, U.hround);
+                scan_frontier<F32>(a, t, a.ws.ring + (size_t)(U.b % kNB) * n,
+                                   min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), ncap), U.b, true, true,
+                                   U.hround, imp);
                 break;
             case kPhLight:
-                scan_frontier(a, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                              min(__ldcg(&ctl->fq_cnt[U.epoch % 3u]), ncap), kTagInit, true, true, U.hround);
+                scan_frontier<F32>(a, t, a.ws.fq + (size_t)(U.epoch % 3u) * n,
+                                   min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), ncap), kTagInit, true, true,
+                                   U.hround, imp);
                 break;
             case kPhHeavy:
-                scan_frontier(a, a.ws.S + (size_t)(U.hround & 1u) * n,
-                              min(__ldcg(&ctl->s_cnt[U.hround & 1u]), ncap), kTagInit, false, false, U.hround);
+                scan_frontier<F32>(a, t, a.ws.S + (size_t)(U.hround & 1u) * n,
+                                   min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), ncap), kTagInit, false, false,
+                                   U.hround, imp);
                 break;
             case kPhEdges:
-                relax_edges<F32>(a, t, min(__ldcg(&ctl->desc_cnt), a.ws.desc_cap), imp);
+                relax_descriptors<F32>(a, t, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
                 break;
             case kPhPending:
                 ++nscans;
