@@ -27,11 +27,11 @@
 //          scanning warp; longer rows become edge descriptors {u, dist(u),
 //          first, end} of at most kDescEdges edges (the reference's request
 //          list R, without one triple per edge).
-//   EDGES  only if descriptors exist: one warp per 32 descriptors.
-// Relaxation is warp-collective: the warp's edge ranges are flattened by a
-// prefix sum and relaxed kUnroll x 32 edges per round, with every load of a
-// round issued before any is used and one counter atomic per target list per
-// round.
+//   EDGES  only if descriptors exist: one warp per descriptor.
+// Relaxation is warp-collective, kUnroll x 32 edges per round (short rows of
+// a SCAN are flattened by a warp prefix sum): every load and every atomic of
+// a round is issued before any result is used, and the targets that improved
+// are appended with one counter atomic per target list per round.
 #pragma once
 
 #include "gbs_internal.cuh"
@@ -75,6 +75,8 @@ __device__ __forceinline__ uint32_t bucket_of(uint32_t dbits, const SsspArgs &a)
     }
 }
 
+constexpr int kQueues = kNB + 2;   // next frontier, kNB ring lists, pending
+
 // Targets of one phase's appends.
 struct Targets {
     uint32_t cur_hi;      // buckets < cur_hi belong to the current bucket
@@ -82,6 +84,7 @@ struct Targets {
     uint32_t stamp_next;
     uint32_t fq_next;     // index of the next-frontier list
     uint32_t pend_sel;    // pending list to append to
+    uint32_t *bins;       // this warp's shared-memory scratch: 2 x kQueues words
 };
 
 // Queue ids: -1 none, 0 next frontier, 1..kNB ring slots, kNB+1 pending.
@@ -98,52 +101,45 @@ __device__ __forceinline__ uint32_t *queue_list(const SsspArgs &a, const Targets
     return a.ws.pend + (size_t)t.pend_sel * n;
 }
 
-// Appends every (q[j], v[j]) with q[j] >= 0 of the whole warp: one pass per
-// distinct target list, one counter atomic per pass.
+// Appends every (q[j], v[j]) with q[j] >= 0 of the whole warp.  A
+// shared-memory histogram over the kQueues target lists gives each item its
+// rank; then lanes reserve space for all non-empty lists at once (one global
+// atomic per list, all in flight together) and every item is written.
 template <int U>
 __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t, const int (&q)[U],
                                              const uint32_t (&v)[U]) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
-    unsigned pend = 0;
+    unsigned has = 0;
 #pragma unroll
-    for (int j = 0; j < U; ++j) pend |= (q[j] >= 0 ? 1u : 0u) << j;
-    for (;;) {
-        const unsigned any = __ballot_sync(FULL, pend != 0);
-        if (!any) break;
-        int myq = -1;
+    for (int j = 0; j < U; ++j) has |= (q[j] >= 0 ? 1u : 0u) << j;
+    if (__ballot_sync(FULL, has != 0) == 0) return;
+    uint32_t *cnt = t.bins, *base = t.bins + kQueues;
+    for (int i = (int)lane; i < kQueues; i += 32) cnt[i] = 0;
+    __syncwarp();
+    uint32_t rank[U];
 #pragma unroll
-        for (int j = U - 1; j >= 0; --j)
-            if ((pend >> j) & 1u) myq = q[j];
-        const int Q = __shfl_sync(FULL, myq, __ffs(any) - 1);
-        unsigned mb = 0;
+    for (int j = 0; j < U; ++j) rank[j] = ((has >> j) & 1u) ? atomicAdd(&cnt[q[j]], 1u) : 0u;
+    __syncwarp();
+    const int i0 = (int)lane, i1 = (int)lane + 32, i2 = (int)lane + 64;
+    const uint32_t c0 = cnt[i0], c1 = cnt[i1], c2 = i2 < kQueues ? cnt[i2] : 0u;
+    const uint32_t b0 = c0 ? atomicAdd(queue_counter(a, t, i0), c0) : 0u;
+    const uint32_t b1 = c1 ? atomicAdd(queue_counter(a, t, i1), c1) : 0u;
+    const uint32_t b2 = c2 ? atomicAdd(queue_counter(a, t, i2), c2) : 0u;
+    if (c0) base[i0] = b0;
+    if (c1) base[i1] = b1;
+    if (c2) base[i2] = b2;
+    __syncwarp();
+    const uint32_t n = a.g.n;
 #pragma unroll
-        for (int j = 0; j < U; ++j) mb |= (((pend >> j) & 1u) && q[j] == Q ? 1u : 0u) << j;
-        const uint32_t c = (uint32_t)__popc(mb);
-        uint32_t incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, o);
-            if ((int)lane >= o) incl += y;
+    for (int j = 0; j < U; ++j) {
+        if ((has >> j) & 1u) {
+            const uint32_t pos = base[q[j]] + rank[j];
+            if (pos < n) queue_list(a, t, q[j])[pos] = v[j];
+            else atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
         }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        uint32_t base = 0;
-        if (lane == 31) base = atomicAdd(queue_counter(a, t, Q), total);
-        base = __shfl_sync(FULL, base, 31) + incl - c;
-        if (mb) {
-            uint32_t *buf = queue_list(a, t, Q);
-            const uint32_t n = a.g.n;
-#pragma unroll
-            for (int j = 0; j < U; ++j) {
-                if ((mb >> j) & 1u) {
-                    if (base < n) buf[base] = v[j];
-                    else atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
-                    ++base;
-                }
-            }
-        }
-        pend &= ~mb;
     }
+    __syncwarp();
 }
 
 // Appends v to one list for every lane with flag set (warp-aggregated).
@@ -176,19 +172,80 @@ __device__ __forceinline__ bool edge_sum(uint32_t du, uint32_t wbits, uint32_t &
     return s < 0xFFFFFFFFull;
 }
 
-// The packed atomicMin lowered v's distance to nd: pick the list v joins.
-template <bool F32>
-__device__ __forceinline__ int classify_improved(const SsspArgs &a, const Targets &t, uint32_t v,
-                                                 uint32_t nd) {
-    const uint32_t nb = bucket_of<F32>(nd, a);
-    if (nb < t.cur_hi) {
-        atomicMin(a.ws.tag + v, nb);
-        return atomicExch(a.ws.fst + v, t.stamp_next) != t.stamp_next ? 0 : -1;
+// Relaxes U candidate edges (u[j] -> v[j], tentative distance nd[j],
+// cand[j] = passed the read-only filter) and returns in q[j] the list each
+// improved target joins.  Every step issues its U atomics before using any
+// result, so they are in flight together:
+//   1. packed (dist << 32 | pred) atomicMin: did the distance drop?
+//   2. dedup: same bucket -> frontier stamp; window -> smallest queued
+//      bucket (tag); beyond the window -> pending (tag = kTagPending)
+template <bool F32, int U>
+__device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &t, const bool (&cand)[U],
+                                              const uint32_t (&v)[U], const uint32_t (&uo)[U],
+                                              const uint32_t (&nd)[U], int (&q)[U], uint32_t &imp) {
+    unsigned long long old[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j)
+        old[j] = cand[j] ? atomicMin(a.ws.dp + v[j], ((unsigned long long)nd[j] << 32) | uo[j]) : 0ull;
+    uint32_t nb[U], kind[U], r[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+        const unsigned long long packed = ((unsigned long long)nd[j] << 32) | uo[j];
+        const bool dec = cand[j] && packed < old[j] && nd[j] < (uint32_t)(old[j] >> 32);
+        imp += dec ? 1u : 0u;
+        nb[j] = dec ? bucket_of<F32>(nd[j], a) : 0u;
+        kind[j] = !dec ? 0u
+                : nb[j] < t.cur_hi ? 1u
+                : (unsigned long long)nb[j] < (unsigned long long)t.W + kNB ? 2u : 3u;
     }
-    if ((unsigned long long)nb < (unsigned long long)t.W + kNB)
-        return atomicMin(a.ws.tag + v, nb) > nb ? 1 + (int)(nb % kNB) : -1;
-    atomicMin(&a.ws.ctl->pend_min[t.pend_sel].v, nb);
-    return atomicMin(a.ws.tag + v, kTagPending) == kTagInit ? kNB + 1 : -1;
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+        r[j] = 0;
+        if (kind[j] == 1u) {
+            atomicMin(a.ws.tag + v[j], nb[j]);
+            r[j] = atomicExch(a.ws.fst + v[j], t.stamp_next);
+        } else if (kind[j] == 2u) {
+            r[j] = atomicMin(a.ws.tag + v[j], nb[j]);
+        } else if (kind[j] == 3u) {
+            atomicMin(&a.ws.ctl->pend_min[t.pend_sel].v, nb[j]);
+            r[j] = atomicMin(a.ws.tag + v[j], kTagPending);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+        q[j] = -1;
+        if (kind[j] == 1u && r[j] != t.stamp_next) q[j] = 0;
+        else if (kind[j] == 2u && r[j] > nb[j]) q[j] = 1 + (int)(nb[j] % kNB);
+        else if (kind[j] == 3u && r[j] == kTagInit) q[j] = kNB + 1;
+    }
+}
+
+// Warp-collective tail of one relaxation round: U edges per lane whose
+// targets and weights are loaded (val[j] = the lane has an edge in slot j).
+template <bool F32, int U>
+__device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Targets &t, const bool (&val)[U],
+                                                 const uint32_t (&v)[U], const uint32_t (&w)[U],
+                                                 const uint32_t (&uo)[U], const uint32_t (&duo)[U],
+                                                 uint32_t &imp) {
+    unsigned long long cur[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
+    bool cand[U];
+    uint32_t nd[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+        cand[j] = false;
+        nd[j] = 0;
+        if (!val[j]) continue;
+        if (!edge_sum<F32>(duo[j], w[j], nd[j])) {
+            atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
+            continue;
+        }
+        cand[j] = (((unsigned long long)nd[j] << 32) | uo[j]) < cur[j];
+    }
+    int q[U];
+    improve_batch<F32, U>(a, t, cand, v, uo, nd, q, imp);
+    warp_enqueue<U>(a, t, q, v);
 }
 
 // Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
@@ -232,27 +289,7 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
                 w[j] = ew.y;
             }
         }
-        unsigned long long cur[kUnroll];
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
-        int q[kUnroll];
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j) {
-            q[j] = -1;
-            uint32_t nd;
-            if (!val[j]) continue;
-            if (!edge_sum<F32>(duo[j], w[j], nd)) {
-                atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
-                continue;
-            }
-            const unsigned long long packed = ((unsigned long long)nd << 32) | uo[j];
-            if (packed >= cur[j]) continue;
-            const unsigned long long old = atomicMin(a.ws.dp + v[j], packed);
-            if (packed >= old || nd >= (uint32_t)(old >> 32)) continue;  // no distance decrease
-            ++imp;
-            q[j] = classify_improved<F32>(a, t, v[j], nd);
-        }
-        warp_enqueue<kUnroll>(a, t, q, v);
+        relax_candidates<F32>(a, t, val, v, w, uo, duo, imp);
     }
 }
 
@@ -320,24 +357,38 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const uint32_
 }
 
 // ------------------------------------------------------------------ EDGES
+// One warp per descriptor (<= kDescEdges edges of one row = one round).
 template <bool F32>
 __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, uint32_t count, uint32_t &imp) {
     const unsigned lane = lane_id();
     const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t groups = (count + 31u) / 32u;
-    for (uint32_t g = warp_g; g < groups; g += nwarps) {
-        const uint32_t idx = g * 32u + lane;
-        uint4 d = make_uint4(0, 0, 0, 0);
-        if (idx < count) d = __ldcg(a.ws.desc + idx);
-        relax_group<F32>(a, t, d.x, d.y, d.z, d.w - d.z, imp);
+    for (uint32_t c = warp_g; c < count; c += nwarps) {
+        const uint4 d = __ldcg(a.ws.desc + c);
+        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+        bool val[kUnroll];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) {
+            const uint32_t e = d.z + 32u * j + lane;
+            val[j] = e < d.w;
+            uo[j] = d.x;
+            duo[j] = d.y;
+            v[j] = 0;
+            w[j] = 0;
+            if (val[j]) {
+                const uint2 ew = ld_stream(a.g.adj + e);
+                v[j] = ew.x;
+                w[j] = ew.y;
+            }
+        }
+        relax_candidates<F32>(a, t, val, v, w, uo, duo, imp);
     }
 }
 
 // Moves pending vertices whose bucket entered the window [W, W+kNB) into the
 // ring; the rest go to the other pending list.
 template <bool F32>
-__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U) {
+__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, uint32_t *bins) {
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
     const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
@@ -348,6 +399,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U) {
     t.stamp_next = 0;
     t.fq_next = 0;
     t.pend_sel = U.pend_sel ^ 1u;
+    t.bins = bins;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
     for (uint32_t base = tid - lane_id(); base < count; base += nthreads) {
@@ -559,6 +611,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     uint32_t imp = 0, nphases = 0, nbuckets = 0, nscans = 0;
     const uint32_t ncap = a.g.n;   // every vertex list holds at most n entries
     __shared__ uint32_t s_next[2];
+    __shared__ uint32_t s_bins[kTPB / 32][2 * kQueues];
+    uint32_t *bins = s_bins[threadIdx.x >> 5];
 
     while (U.phase != kPhDone) {
         Targets t;
@@ -567,6 +621,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
         t.stamp_next = U.epoch + 1;
         t.fq_next = (U.epoch + 1) % 3u;
         t.pend_sel = U.pend_sel;
+        t.bins = bins;
         const uint32_t n = a.g.n;
         switch (U.phase) {
             case kPhLightFirst:
@@ -590,7 +645,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
                 break;
             case kPhPending:
                 ++nscans;
-                rebucket_pending<F32>(a, U);
+                rebucket_pending<F32>(a, U, bins);
                 break;
             default:
                 break;
