@@ -76,6 +76,15 @@ __device__ __forceinline__ uint32_t bucket_of(uint32_t dbits, const SsspArgs &a)
 }
 
 constexpr int kQueues = kNB + 2;   // next frontier, kNB ring lists, pending
+constexpr int kCand = 64;          // candidate buffer: < 32 kept + <= 32 per append
+
+// Per-warp shared-memory scratch.
+struct WarpScratch {
+    uint32_t bins[2 * kQueues];    // enqueue histogram and list bases
+    uint32_t cv[kCand];            // candidate target
+    uint32_t cnd[kCand];           // candidate tentative distance bits
+    uint32_t cu[kCand];            // candidate source
+};
 
 // Targets of one phase's appends.
 struct Targets {
@@ -84,7 +93,7 @@ struct Targets {
     uint32_t stamp_next;
     uint32_t fq_next;     // index of the next-frontier list
     uint32_t pend_sel;    // pending list to append to
-    uint32_t *bins;       // this warp's shared-memory scratch: 2 x kQueues words
+    WarpScratch *scr;     // this warp's shared-memory scratch
 };
 
 // Queue ids: -1 none, 0 next frontier, 1..kNB ring slots, kNB+1 pending.
@@ -114,7 +123,7 @@ __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t
 #pragma unroll
     for (int j = 0; j < U; ++j) has |= (q[j] >= 0 ? 1u : 0u) << j;
     if (__ballot_sync(FULL, has != 0) == 0) return;
-    uint32_t *cnt = t.bins, *base = t.bins + kQueues;
+    uint32_t *cnt = t.scr->bins, *base = t.scr->bins + kQueues;
     for (int i = (int)lane; i < kQueues; i += 32) cnt[i] = 0;
     __syncwarp();
     uint32_t rank[U];
@@ -222,37 +231,76 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
 
 // Warp-collective tail of one relaxation round: U edges per lane whose
 // targets and weights are loaded (val[j] = the lane has an edge in slot j).
+// Runs the atomic part (improve_batch + enqueue) on the top `take` (<= 32)
+// candidates of the warp's buffer, one per lane.
+template <bool F32>
+__device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t take,
+                                           uint32_t &imp) {
+    const unsigned lane = lane_id();
+    WarpScratch *s = t.scr;
+    const bool has = lane < take;
+    const uint32_t i = nc - take + lane;
+    uint32_t v1[1] = {has ? s->cv[i] : 0u};
+    uint32_t u1[1] = {has ? s->cu[i] : 0u};
+    uint32_t n1[1] = {has ? s->cnd[i] : 0u};
+    const bool c1[1] = {has};
+    __syncwarp();
+    nc -= take;
+    int q[1];
+    improve_batch<F32, 1>(a, t, c1, v1, u1, n1, q, imp);
+    warp_enqueue<1>(a, t, q, v1);
+}
+
+// Warp-collective tail of one relaxation round: U edges per lane whose
+// targets and weights are loaded (val[j] = the lane has an edge in slot j).
+// Only edges that pass the read-only filter (packed tentative value below
+// the current dp) become candidates; they collect in the warp's shared-memory
+// buffer and the atomic chain runs once per 32 of them, not once per round.
 template <bool F32, int U>
 __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Targets &t, const bool (&val)[U],
                                                  const uint32_t (&v)[U], const uint32_t (&w)[U],
                                                  const uint32_t (&uo)[U], const uint32_t (&duo)[U],
-                                                 uint32_t &imp) {
+                                                 uint32_t &nc, uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
     unsigned long long cur[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) cur[j] = val[j] ? __ldcg(a.ws.dp + v[j]) : 0ull;
-    bool cand[U];
-    uint32_t nd[U];
+    WarpScratch *s = t.scr;
 #pragma unroll
     for (int j = 0; j < U; ++j) {
-        cand[j] = false;
-        nd[j] = 0;
-        if (!val[j]) continue;
-        if (!edge_sum<F32>(duo[j], w[j], nd[j])) {
-            atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
-            continue;
+        bool cand = false;
+        uint32_t nd = 0;
+        if (val[j]) {
+            if (!edge_sum<F32>(duo[j], w[j], nd)) atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
+            else cand = (((unsigned long long)nd << 32) | uo[j]) < cur[j];
         }
-        cand[j] = (((unsigned long long)nd[j] << 32) | uo[j]) < cur[j];
+        const unsigned m = __ballot_sync(FULL, cand);
+        if (m) {
+            if (cand) {
+                const uint32_t p = nc + (uint32_t)__popc(m & ((1u << lane) - 1u));
+                s->cv[p] = v[j];
+                s->cnd[p] = nd;
+                s->cu[p] = uo[j];
+            }
+            nc += (uint32_t)__popc(m);
+            __syncwarp();
+            if (nc >= 32u) cand_flush<F32>(a, t, nc, 32u, imp);
+        }
     }
-    int q[U];
-    improve_batch<F32, U>(a, t, cand, v, uo, nd, q, imp);
-    warp_enqueue<U>(a, t, q, v);
+}
+
+// Drains the warp's candidate buffer (end of a phase's relaxation work).
+template <bool F32>
+__device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t &imp) {
+    if (nc) cand_flush<F32>(a, t, nc, nc, imp);
 }
 
 // Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
 // given by every lane (len may be 0), kUnroll x 32 edges per round.
 template <bool F32>
 __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t, uint32_t u, uint32_t du,
-                                            uint32_t s, uint32_t len, uint32_t &imp) {
+                                            uint32_t s, uint32_t len, uint32_t &nc, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     uint32_t incl = len;
@@ -289,7 +337,7 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
                 w[j] = ew.y;
             }
         }
-        relax_candidates<F32>(a, t, val, v, w, uo, duo, imp);
+        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
     }
 }
 
@@ -306,23 +354,26 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const uint32_
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
     uint32_t my_edges = 0;
+    uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t base = tid - lane; base < count; base += nthreads) {
         const uint32_t i = base + lane;
         uint32_t u = 0, du = 0, s = 0, e = 0;
         bool ok = false;
         if (i < count) {
             u = __ldcg(F + i);
-            ok = (vtag == kTagInit) || (__ldcg(a.ws.tag + u) == vtag);
-        }
-        if (ok) {
+            // the tag check and the row reads are independent: issue together
+            const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
             du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
             const uint32_t md = __ldg(a.ws.mid + u);
-            s = light ? __ldg(a.g.row + u) : md;
-            e = light ? md : __ldg(a.g.row + u + 1);
+            const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
+            ok = tg == vtag;
+            s = ok ? (light ? r : md) : 0u;
+            e = ok ? (light ? md : r) : 0u;
         }
-        bool sflag = false;
-        if (ok && add_s) sflag = atomicExch(a.ws.hst + u, hround) != hround;
-        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n, sflag, u, ctl);
+        // S membership is decided now; the append waits until after the
+        // relaxation below so its latency overlaps that work
+        uint32_t hold = hround;
+        if (ok && add_s) hold = atomicExch(a.ws.hst + u, hround);
         const uint32_t len = e - s;
         // long rows -> descriptors, reserved with one atomic per warp
         const uint32_t nd = len > kInlineEdges ? (len + kDescEdges - 1) / kDescEdges : 0u;
@@ -349,8 +400,11 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const uint32_
             my_edges += nd ? len : 0u;
         }
         // short rows: relaxed by this warp now
-        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, imp);
+        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, nc, imp);
+        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n,
+                    ok && add_s && hold != hround, u, ctl);
     }
+    cand_drain<F32>(a, t, nc, imp);
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
     if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
@@ -363,6 +417,7 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, uint32_t 
     const unsigned lane = lane_id();
     const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t c = warp_g; c < count; c += nwarps) {
         const uint4 d = __ldcg(a.ws.desc + c);
         uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
@@ -381,14 +436,15 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, uint32_t 
                 w[j] = ew.y;
             }
         }
-        relax_candidates<F32>(a, t, val, v, w, uo, duo, imp);
+        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
     }
+    cand_drain<F32>(a, t, nc, imp);
 }
 
 // Moves pending vertices whose bucket entered the window [W, W+kNB) into the
 // ring; the rest go to the other pending list.
 template <bool F32>
-__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, uint32_t *bins) {
+__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, WarpScratch *scr) {
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
     const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
@@ -399,7 +455,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, uint32_t *
     t.stamp_next = 0;
     t.fq_next = 0;
     t.pend_sel = U.pend_sel ^ 1u;
-    t.bins = bins;
+    t.scr = scr;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
     for (uint32_t base = tid - lane_id(); base < count; base += nthreads) {
@@ -611,8 +667,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     uint32_t imp = 0, nphases = 0, nbuckets = 0, nscans = 0;
     const uint32_t ncap = a.g.n;   // every vertex list holds at most n entries
     __shared__ uint32_t s_next[2];
-    __shared__ uint32_t s_bins[kTPB / 32][2 * kQueues];
-    uint32_t *bins = s_bins[threadIdx.x >> 5];
+    __shared__ WarpScratch s_scr[kTPB / 32];
+    WarpScratch *scr = &s_scr[threadIdx.x >> 5];
 
     while (U.phase != kPhDone) {
         Targets t;
@@ -621,7 +677,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
         t.stamp_next = U.epoch + 1;
         t.fq_next = (U.epoch + 1) % 3u;
         t.pend_sel = U.pend_sel;
-        t.bins = bins;
+        t.scr = scr;
         const uint32_t n = a.g.n;
         switch (U.phase) {
             case kPhLightFirst:
@@ -645,7 +701,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
                 break;
             case kPhPending:
                 ++nscans;
-                rebucket_pending<F32>(a, U, bins);
+                rebucket_pending<F32>(a, U, scr);
                 break;
             default:
                 break;
