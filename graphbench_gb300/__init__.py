@@ -34,7 +34,8 @@ F_NO_STATS = 0x1
 EXPORTS = [
     "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
-    "gbs_sssp_multi", "gbs_trace", "gbs_host_alloc", "gbs_host_free", "gbs_device_alloc", "gbs_device_free",
+    "gbs_sssp_multi", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
+    "gbs_device_alloc", "gbs_device_free",
     "gbs_device_synchronize",
     "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
 ]
@@ -109,6 +110,9 @@ def _load() -> ctypes.CDLL:
     L.gbs_sample_sources.argtypes = [ctypes.POINTER(HostCsr), ctypes.c_uint32, ctypes.c_uint64, P, P]
     L.gbs_host_csr_free.argtypes = [ctypes.POINTER(HostCsr)]
     L.gbs_trace.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+    # no-allocation variant: device pointers in, device pointers out
+    L.gbs_sssp_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_uint64, P, P, ctypes.c_int, ctypes.c_uint32,
+                                   ctypes.c_double, P, P, P]
     return L
 
 

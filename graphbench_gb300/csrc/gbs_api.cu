@@ -30,6 +30,12 @@ gbs_status fail(gbs_status s, const std::string &msg) {
     return s;
 }
 
+}  // namespace
+
+void gbs::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+namespace {
+
 #define GBS_CUDA(call)                                                                       \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \

@@ -152,4 +152,7 @@ __device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
 }
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Sets the message gbs_last_error returns on the calling thread.
+void set_last_error(const char *msg);
+
 }  // namespace gbs

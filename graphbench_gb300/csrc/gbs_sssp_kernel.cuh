@@ -486,7 +486,7 @@ __device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
 // Run by warp 0 of the CTA that arrives last at a barrier: every other CTA
 // has finished the phase, so all counters are at rest.  Decides the next
 // phase, resets the lists that phase will append to, and publishes.
-__device__ void control_step(const SsspArgs &a, const Uniform &U) {
+__device__ inline void control_step(const SsspArgs &a, const Uniform &U) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();

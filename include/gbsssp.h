@@ -167,6 +167,32 @@ typedef struct gbs_phase_rec {
 
 gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *count);
 
+/*
+ * SSSP that allocates no memory (no counterpart in the reference).  For
+ * callers that cannot call cudaMalloc/cudaFree while serving a query: a host
+ * application that owns all device memory through its own pool, or a
+ * latency-bound service for which an allocation (which may synchronise the
+ * device or fail with out-of-memory mid-request) is not acceptable.  The
+ * caller passes device buffers it owns:
+ *   row_dev  n+1 uint32 exclusive row offsets (row_dev[0] = 0, row_dev[n] = m)
+ *   adj_dev  2*m uint32: per edge {target, weight bits}, rows in any order
+ *   dist_dev n uint32/float32 distances (required), pred_dev n int32 (may be NULL)
+ * Weights are uint32 or float32 (>= 0) per wtype; delta <= 0 selects max
+ * weight / average out-degree.  Results equal gbs_sssp's bit for bit.
+ * Everything else lives in one static device array of about 21 MB that the
+ * library holds on every GPU that loads it: n must be at most 65,536 and m at
+ * most 2,097,152 (larger inputs return GBS_ERR_INVALID_ARG).  The input CSR is
+ * validated on the device first (GBS_ERR_INVALID_ARG if malformed).  Runs on
+ * `stream` (a cudaStream_t, NULL = default stream) and returns when done.
+ * The first call on a device (with that device current) looks up the static
+ * array's address and caches it; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.
+ */
+gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *row_dev,
+                            const uint32_t *adj_dev, gbs_weight_type wtype, uint32_t source,
+                            double delta, void *dist_dev, int32_t *pred_dev, void *stream);
+
 /* Pinned host memory for fast transfers. */
 gbs_status gbs_host_alloc(size_t bytes, void **out);
 gbs_status gbs_host_free(void *p);
