@@ -51,7 +51,7 @@ class GbsError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
                 ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("solo_entries", ctypes.c_uint32), ("solo_descs", ctypes.c_uint32)]
 
 
 class PhaseRec(ctypes.Structure):
@@ -61,6 +61,7 @@ class PhaseRec(ctypes.Structure):
 
 PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "scan_heavy", 3: "relax", 4: "pending"}
 F_TRACE = 0x2
+F_NO_SOLO = 0x4
 F_TEST_STALL = 0x80000000
 
 
@@ -70,7 +71,8 @@ class Stats(ctypes.Structure):
                 ("improvements", ctypes.c_uint64), ("buckets", ctypes.c_uint32),
                 ("phases", ctypes.c_uint32), ("pending_scans", ctypes.c_uint32),
                 ("blocks", ctypes.c_uint32), ("delta_used", ctypes.c_double),
-                ("light_used", ctypes.c_double)]
+                ("light_used", ctypes.c_double), ("solo_phases", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -302,12 +304,14 @@ class Graph:
 
     @staticmethod
     def params(delta: float | None = None, light: float | None = None, flags: int = 0,
-               wait_limit_ms: int = 0) -> Params:
+               wait_limit_ms: int = 0, solo_entries: int = 0, solo_descs: int = 0) -> Params:
         p = Params()
         p.delta = float(delta) if delta else 0.0
         p.light = float(light) if light is not None else -1.0
         p.flags = flags
         p.wait_limit_ms = wait_limit_ms
+        p.solo_entries = solo_entries
+        p.solo_descs = solo_descs
         return p
 
     def trace(self) -> list[dict]:
@@ -316,8 +320,9 @@ class Graph:
         _check(lib.gbs_trace(self._h, None, 0, ctypes.byref(cnt)), "gbs_trace")
         recs = (PhaseRec * max(1, cnt.value))()
         _check(lib.gbs_trace(self._h, recs, cnt.value, ctypes.byref(cnt)), "gbs_trace")
-        return [{"kind": PHASE_KINDS.get(r.kind, r.kind), "bucket": r.bucket, "items": r.items,
-                 "edges": r.edges, "end_ns": r.end_ns} for r in recs[: cnt.value]]
+        return [{"kind": PHASE_KINDS.get(r.kind & 15, r.kind), "solo": bool(r.kind & 16),
+                 "bucket": r.bucket, "items": r.items, "edges": r.edges, "end_ns": r.end_ns}
+                for r in recs[: cnt.value]]
 
     def sssp(self, source: int, delta: float | None = None, light: float | None = None,
              out_dist: np.ndarray | None = None, out_pred: np.ndarray | None = None,

@@ -4,7 +4,7 @@
 // One run on the graph's stream:
 //   [mid]   first-heavy-edge index per row, only when the light split changes
 //   reset   dp = unreached, tag = none, control block, source in ring bucket 0
-//   persistent cooperative kernel (gbs_sssp_kernel.cuh)
+//   persistent cooperative kernel (gbs_sssp_persistent.cuh)
 //   unpack  dp -> dist / pred in the caller's layout
 //   [stats] reached vertices and edges (the GTEPS numerator)
 #include <algorithm>
@@ -17,7 +17,7 @@
 #include <thread>
 #include <vector>
 
-#include "gbs_sssp_kernel.cuh"
+#include "gbs_sssp_persistent.cuh"
 
 using namespace gbs;
 
@@ -69,8 +69,8 @@ __global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restric
         ctl->ring_cnt[0].v = 1;
         ctl->pend_min[0].v = kTagInit;
         ctl->pend_min[1].v = kTagInit;
-        ctl->mode = kPhLightFirst;
-        ctl->next_bucket = 0;
+        ctl->pub_phase = kPhLightFirst;
+        ctl->pub_b = 0;
     }
 }
 
@@ -290,6 +290,9 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.inv_delta_f = r.inv_delta_f;
     a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
     a.flags = p ? p->flags : 0u;
+    const bool no_solo = (a.flags & GBS_F_NO_SOLO) != 0;
+    a.solo_items = no_solo ? 0u : ((p && p->solo_entries) ? p->solo_entries : 1024u);
+    a.solo_desc = no_solo ? 0u : ((p && p->solo_descs) ? p->solo_descs : 64u);
     a.run_ns = a.wait_ns * 16ull;
     if (a.flags & GBS_F_TRACE) {
         if (!g->ws.trace) {
@@ -352,6 +355,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
         stats->phases = c.st_phases;
         stats->pending_scans = c.st_pending_scans;
         stats->blocks = (uint32_t)g->blocks;
+        stats->solo_phases = c.st_solo_phases;
         stats->delta_used = r.delta;
         stats->light_used = r.light;
     }

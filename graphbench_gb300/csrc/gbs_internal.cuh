@@ -68,10 +68,17 @@ struct __align__(128) Ctl {
     uint32_t bar_gen;
     uint32_t pad1[31];
     uint32_t error;
-    uint32_t mode;          // decision published by the last CTA at a barrier
-    uint32_t next_bucket;
     uint32_t trace_n;
-    uint32_t pad2[28];
+    // kernel state published by the deciding CTA at each barrier: the next
+    // phase and everything the CTAs need to run it
+    uint32_t pub_phase;
+    uint32_t pub_logical;
+    uint32_t pub_b;
+    uint32_t pub_W;
+    uint32_t pub_epoch;
+    uint32_t pub_hround;
+    uint32_t pub_pend_sel;
+    uint32_t pad2[23];
     Line ring_cnt[kNB];
     Line fq_cnt[3];
     Line s_cnt[2];
@@ -85,7 +92,7 @@ struct __align__(128) Ctl {
     uint32_t st_pending_scans;
     uint32_t next_epoch;
     uint32_t next_hround;
-    uint32_t pad4;
+    uint32_t st_solo_phases;      // phases run by one CTA without a grid barrier
     unsigned long long st_improvements;
     unsigned long long st_reached;
     unsigned long long st_edges_reached;
@@ -120,6 +127,8 @@ struct SsspArgs {
     uint32_t delta_u;       // uint32 bucket width (>= 1)
     float inv_delta_f;      // float32: bucket = floor(d * inv_delta)
     uint32_t flags;         // GBS_F_* of the call
+    uint32_t solo_items;    // a SCAN/PENDING phase with at most this many entries runs on one CTA
+    uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
     unsigned long long wait_ns;   // limit of one barrier wait
     unsigned long long run_ns;    // limit of the whole run
 };

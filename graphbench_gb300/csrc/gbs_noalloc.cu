@@ -31,7 +31,7 @@
 #include <mutex>
 #include <string>
 
-#include "gbs_sssp_kernel.cuh"
+#include "gbs_sssp_persistent.cuh"
 
 using namespace gbs;
 
@@ -91,8 +91,8 @@ __global__ void k_noalloc_reset(unsigned long long *__restrict__ dp, uint32_t *_
         ctl->ring_cnt[0].v = 1;
         ctl->pend_min[0].v = kTagInit;
         ctl->pend_min[1].v = kTagInit;
-        ctl->mode = kPhLightFirst;
-        ctl->next_bucket = 0;
+        ctl->pub_phase = kPhLightFirst;
+        ctl->pub_b = 0;
     }
 }
 
@@ -230,6 +230,8 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.delta_u = (uint32_t)std::min(std::max(std::floor(delta), 1.0), 4294967295.0);
     a.inv_delta_f = (float)(1.0 / delta);
     a.flags = 0;
+    a.solo_items = 1024;
+    a.solo_desc = 64;
     a.wait_ns = 4000ull * 1000000ull;
     a.run_ns = a.wait_ns * 16ull;
 

@@ -341,392 +341,5 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
     }
 }
 
-// ------------------------------------------------------------------- SCAN
-// One thread per frontier entry.  vtag != kTagInit keeps only entries whose
-// tag equals it (ring lists may hold entries that moved to a lower bucket).
-template <bool F32>
-__device__ void scan_frontier(const SsspArgs &a, const Targets &t, const uint32_t *F, uint32_t count,
-                              uint32_t vtag, bool light, bool add_s, uint32_t hround, uint32_t &imp) {
-    const unsigned FULL = 0xffffffffu;
-    const unsigned lane = lane_id();
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
-    const uint32_t n = a.g.n;
-    Ctl *ctl = a.ws.ctl;
-    uint32_t my_edges = 0;
-    uint32_t nc = 0;   // candidates buffered by this warp
-    for (uint32_t base = tid - lane; base < count; base += nthreads) {
-        const uint32_t i = base + lane;
-        uint32_t u = 0, du = 0, s = 0, e = 0;
-        bool ok = false;
-        if (i < count) {
-            u = __ldcg(F + i);
-            // the tag check and the row reads are independent: issue together
-            const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
-            du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
-            const uint32_t md = __ldg(a.ws.mid + u);
-            const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
-            ok = tg == vtag;
-            s = ok ? (light ? r : md) : 0u;
-            e = ok ? (light ? md : r) : 0u;
-        }
-        // S membership is decided now; the append waits until after the
-        // relaxation below so its latency overlaps that work
-        uint32_t hold = hround;
-        if (ok && add_s) hold = atomicExch(a.ws.hst + u, hround);
-        const uint32_t len = e - s;
-        // long rows -> descriptors, reserved with one atomic per warp
-        const uint32_t nd = len > kInlineEdges ? (len + kDescEdges - 1) / kDescEdges : 0u;
-        uint32_t incl = nd;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, o);
-            if ((int)lane >= o) incl += y;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        if (total) {
-            uint32_t dbase = 0;
-            if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt.v, total);
-            dbase = __shfl_sync(FULL, dbase, 31);
-            const uint32_t pos = dbase + incl - nd;
-            if (pos + nd <= a.ws.desc_cap) {
-                for (uint32_t c = 0; c < nd; ++c) {
-                    const uint32_t cs = s + c * kDescEdges;
-                    a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
-                }
-            } else if (nd) {
-                atomicExch(&ctl->error, (uint32_t)kErrCapacity);
-            }
-            my_edges += nd ? len : 0u;
-        }
-        // short rows: relaxed by this warp now
-        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, nc, imp);
-        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n,
-                    ok && add_s && hold != hround, u, ctl);
-    }
-    cand_drain<F32>(a, t, nc, imp);
-    // edges handed to EDGES (statistics / trace)
-    for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
-    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
-}
-
-// ------------------------------------------------------------------ EDGES
-// One warp per descriptor (<= kDescEdges edges of one row = one round).
-template <bool F32>
-__device__ void relax_descriptors(const SsspArgs &a, const Targets &t, uint32_t count, uint32_t &imp) {
-    const unsigned lane = lane_id();
-    const uint32_t warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    uint32_t nc = 0;   // candidates buffered by this warp
-    for (uint32_t c = warp_g; c < count; c += nwarps) {
-        const uint4 d = __ldcg(a.ws.desc + c);
-        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
-        bool val[kUnroll];
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j) {
-            const uint32_t e = d.z + 32u * j + lane;
-            val[j] = e < d.w;
-            uo[j] = d.x;
-            duo[j] = d.y;
-            v[j] = 0;
-            w[j] = 0;
-            if (val[j]) {
-                const uint2 ew = ld_stream(a.g.adj + e);
-                v[j] = ew.x;
-                w[j] = ew.y;
-            }
-        }
-        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
-    }
-    cand_drain<F32>(a, t, nc, imp);
-}
-
-// Moves pending vertices whose bucket entered the window [W, W+kNB) into the
-// ring; the rest go to the other pending list.
-template <bool F32>
-__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, WarpScratch *scr) {
-    const uint32_t n = a.g.n;
-    Ctl *ctl = a.ws.ctl;
-    const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
-    const uint32_t *list = a.ws.pend + (size_t)U.pend_sel * n;
-    Targets t;
-    t.cur_hi = 0;
-    t.W = U.W;
-    t.stamp_next = 0;
-    t.fq_next = 0;
-    t.pend_sel = U.pend_sel ^ 1u;
-    t.scr = scr;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
-    for (uint32_t base = tid - lane_id(); base < count; base += nthreads) {
-        const uint32_t i = base + lane_id();
-        int q[1] = {-1};
-        uint32_t v[1] = {0};
-        if (i < count) {
-            v[0] = __ldcg(list + i);
-            if (__ldcg(a.ws.tag + v[0]) == kTagPending) {
-                const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v[0]) >> 32), a);
-                if ((unsigned long long)nb < (unsigned long long)U.W + kNB) {
-                    a.ws.tag[v[0]] = nb;
-                    q[0] = 1 + (int)(nb % kNB);
-                } else {
-                    atomicMin(&ctl->pend_min[t.pend_sel].v, nb);
-                    q[0] = kNB + 1;
-                }
-            }
-        }
-        warp_enqueue<1>(a, t, q, v);
-    }
-}
-
-__device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
-    return phase == kPhHeavy ? (uint32_t)kPhHeavy : (uint32_t)kPhLight;
-}
-
-// Run by warp 0 of the CTA that arrives last at a barrier: every other CTA
-// has finished the phase, so all counters are at rest.  Decides the next
-// phase, resets the lists that phase will append to, and publishes.
-__device__ inline void control_step(const SsspArgs &a, const Uniform &U) {
-    Ctl *ctl = a.ws.ctl;
-    const unsigned FULL = 0xffffffffu;
-    const unsigned lane = lane_id();
-    // one round trip: every counter the decision needs is loaded at once
-    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane].v);
-    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32].v);
-    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt.v);
-    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u].v);
-    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0].v), pc1 = ld_relaxed(&ctl->pend_cnt[1].v);
-    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0].v), pm1 = ld_relaxed(&ctl->pend_min[1].v);
-    const uint32_t err = ld_relaxed(&ctl->error);
-
-    uint32_t next = kPhDone, nb = 0;
-    uint32_t e2 = U.epoch, h2 = U.hround, ps2 = U.pend_sel;
-    bool need_ring_scan = false;
-    uint32_t scan_from = 0;
-    if (U.phase == kPhPending) {
-        ps2 ^= 1u;
-        need_ring_scan = true;
-        scan_from = U.W;
-        if (lane == 0) { ctl->pend_cnt[U.pend_sel].v = 0; ctl->pend_min[U.pend_sel].v = kTagInit; }
-    } else if (U.phase != kPhEdges && desc_cnt > 0) {
-        next = kPhEdges;
-    } else {
-        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
-        e2 = U.epoch + 1;
-        if (logical == kPhHeavy) h2 = U.hround + 1;
-        if (fq_next > 0) {
-            next = kPhLight;
-        } else if (logical == kPhLight) {
-            next = kPhHeavy;
-        } else {
-            if (lane == 0) ctl->ring_cnt[U.b % kNB].v = 0;
-            need_ring_scan = true;
-            scan_from = U.b + 1;
-        }
-    }
-    if (need_ring_scan) {
-        // first non-empty ring bucket in [scan_from, W + kNB); at a bucket end
-        // scan_from = b + 1 = W + 1, so the slot just cleared is not read.
-        const uint32_t lim = U.W + kNB;   // exclusive
-        uint32_t found = 0xFFFFFFFFu;
-#pragma unroll
-        for (uint32_t off = 0; off < (uint32_t)kNB; off += 32u) {
-            const uint32_t bk = scan_from + off + lane;
-            const uint32_t slot = bk % kNB;
-            const uint32_t c_lo = __shfl_sync(FULL, ring_lo, slot & 31u);
-            const uint32_t c_hi = __shfl_sync(FULL, ring_hi, slot & 31u);
-            const uint32_t c = slot < 32 ? c_lo : c_hi;
-            const unsigned m = __ballot_sync(FULL, bk < lim && c > 0);
-            if (m && found == 0xFFFFFFFFu) found = scan_from + off + (uint32_t)(__ffs(m) - 1);
-        }
-        const uint32_t pcnt = ps2 ? pc1 : pc0;
-        const uint32_t pm = ps2 ? pm1 : pm0;
-        if (pcnt > 0 && pm <= found) {
-            next = kPhPending;
-            nb = pm;
-        } else if (found != 0xFFFFFFFFu) {
-            next = kPhLightFirst;
-            nb = found;
-        } else {
-            next = kPhDone;
-        }
-    }
-    // whole-run limit: a run that has not finished within run_ns is stopped
-    if (globaltimer() - U.t0 > a.run_ns) {
-        next = kPhDone;
-        if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
-    }
-    if (err) next = kPhDone;
-    if (lane == 0) {
-        if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
-            const uint32_t ti = ctl->trace_n;
-            if (ti < a.ws.trace_cap) {
-                uint32_t items;
-                switch (U.phase) {
-                    case kPhLightFirst: items = ld_relaxed(&ctl->ring_cnt[U.b % kNB].v); break;
-                    case kPhLight: items = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u].v); break;
-                    case kPhHeavy: items = ld_relaxed(&ctl->s_cnt[U.hround & 1u].v); break;
-                    case kPhEdges: items = desc_cnt; break;
-                    default: items = ld_relaxed(&ctl->pend_cnt[U.pend_sel].v); break;
-                }
-                TraceRec r;
-                r.kind = U.phase;
-                r.bucket = U.b;
-                r.items = items;
-                r.edges = ld_relaxed(&ctl->edge_cnt.v);
-                r.end_ns = globaltimer() - U.t0;
-                a.ws.trace[ti] = r;
-            }
-            ctl->trace_n = ti + 1;
-        }
-        if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
-            ctl->fq_cnt[(e2 + 1u) % 3u].v = 0;
-            ctl->desc_cnt.v = 0;
-            ctl->edge_cnt.v = 0;
-            if (h2 != U.hround || next == kPhLightFirst) ctl->s_cnt[h2 & 1u].v = 0;
-        }
-        ctl->mode = next;
-        ctl->next_bucket = nb;
-    }
-    __syncwarp();
-}
-
-// Applies the published decision to the uniform state (identical in all CTAs).
-__device__ __forceinline__ void advance_uniform(Uniform &U, uint32_t next, uint32_t nb) {
-    if (U.phase == kPhPending) {
-        U.pend_sel ^= 1u;
-    } else if (next == kPhEdges) {
-        U.logical = scan_kind(U.phase);
-    } else {
-        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
-        U.epoch += 1;
-        if (logical == kPhHeavy) U.hround += 1;
-    }
-    if (next == kPhLightFirst) { U.b = nb; U.W = nb; }
-    if (next == kPhPending) U.W = nb;
-    U.phase = next;
-}
-
-// Grid barrier; the last CTA to arrive runs control_step before releasing.
-// Waits are bounded by a.wait_ns (globaltimer); on expiry the error flag is
-// set and every CTA leaves at its next check.
-__device__ __forceinline__ void grid_barrier(const SsspArgs &a, Uniform &U) {
-    Ctl *ctl = a.ws.ctl;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t last = 0;
-        // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
-        const bool stall = (a.flags & GBS_F_TEST_STALL) && U.gen == 0 && blockIdx.x == 0;
-        if (threadIdx.x == 0 && !stall) {
-            __threadfence();
-            const uint32_t arrived = atomicAdd(&ctl->bar_count, 1u);
-            last = (arrived == gridDim.x - 1u);
-        }
-        last = __shfl_sync(0xffffffffu, last, 0);
-        if (last) {
-            __threadfence();
-            control_step(a, U);
-            if (threadIdx.x == 0) {
-                ctl->bar_count = 0;
-                __threadfence();
-                st_release(&ctl->bar_gen, U.gen + 1u);
-            }
-        } else if (threadIdx.x == 0) {
-            const unsigned long long t0 = globaltimer();
-            uint32_t spins = 0;
-            while (ld_acquire(&ctl->bar_gen) != U.gen + 1u) {
-                if ((++spins & 255u) == 0) {
-                    if (ld_relaxed(&ctl->error) != 0) break;
-                    if (globaltimer() - t0 > a.wait_ns) {
-                        atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
-                        break;
-                    }
-                }
-            }
-        }
-        __syncwarp();
-        if (threadIdx.x == 0) __threadfence();
-    }
-    __syncthreads();
-    U.gen += 1;
-}
-
-template <bool F32>
-__global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
-    Ctl *ctl = a.ws.ctl;
-    Uniform U;
-    U.phase = ld_relaxed(&ctl->mode);
-    U.logical = kPhLight;
-    U.b = ld_relaxed(&ctl->next_bucket);
-    U.W = U.b;
-    U.epoch = a.epoch0;
-    U.hround = a.hround0;
-    U.pend_sel = 0;
-    U.gen = 0;
-    U.t0 = globaltimer();
-    uint32_t imp = 0, nphases = 0, nbuckets = 0, nscans = 0;
-    const uint32_t ncap = a.g.n;   // every vertex list holds at most n entries
-    __shared__ uint32_t s_next[2];
-    __shared__ WarpScratch s_scr[kTPB / 32];
-    WarpScratch *scr = &s_scr[threadIdx.x >> 5];
-
-    while (U.phase != kPhDone) {
-        Targets t;
-        t.cur_hi = U.b + 1;
-        t.W = U.W;
-        t.stamp_next = U.epoch + 1;
-        t.fq_next = (U.epoch + 1) % 3u;
-        t.pend_sel = U.pend_sel;
-        t.scr = scr;
-        const uint32_t n = a.g.n;
-        switch (U.phase) {
-            case kPhLightFirst:
-                ++nbuckets;
-                scan_frontier<F32>(a, t, a.ws.ring + (size_t)(U.b % kNB) * n,
-                                   min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), ncap), U.b, true, true,
-                                   U.hround, imp);
-                break;
-            case kPhLight:
-                scan_frontier<F32>(a, t, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                                   min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), ncap), kTagInit, true, true,
-                                   U.hround, imp);
-                break;
-            case kPhHeavy:
-                scan_frontier<F32>(a, t, a.ws.S + (size_t)(U.hround & 1u) * n,
-                                   min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), ncap), kTagInit, false, false,
-                                   U.hround, imp);
-                break;
-            case kPhEdges:
-                relax_descriptors<F32>(a, t, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
-                break;
-            case kPhPending:
-                ++nscans;
-                rebucket_pending<F32>(a, U, scr);
-                break;
-            default:
-                break;
-        }
-        grid_barrier(a, U);
-        ++nphases;
-        if (threadIdx.x == 0) {
-            s_next[0] = ld_relaxed(&ctl->error) ? (uint32_t)kPhDone : ld_relaxed(&ctl->mode);
-            s_next[1] = ld_relaxed(&ctl->next_bucket);
-        }
-        __syncthreads();
-        const uint32_t next = s_next[0], nb = s_next[1];
-        __syncthreads();
-        advance_uniform(U, next, nb);
-    }
-    // statistics
-    for (int o = 16; o > 0; o >>= 1) imp += __shfl_down_sync(0xffffffffu, imp, o);
-    if (lane_id() == 0 && imp) atomicAdd(&ctl->st_improvements, (unsigned long long)imp);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        ctl->st_buckets = nbuckets;
-        ctl->st_phases = nphases;
-        ctl->st_pending_scans = nscans;
-        ctl->next_epoch = U.epoch;        // next free stamps for the following run
-        ctl->next_hround = U.hround;
-    }
-}
 
 }  // namespace gbs

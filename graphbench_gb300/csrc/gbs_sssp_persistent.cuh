@@ -1,0 +1,505 @@
+// gbs_sssp_persistent.cuh -- phases, decisions and the persistent kernel.
+//
+// The relaxation machinery (candidate filter, packed atomicMin, list appends)
+// is in gbs_sssp_kernel.cuh.  This file holds the phase bodies, the decision
+// taken at every barrier, the grid barrier itself and the kernel.
+//
+// Phases run either on the whole grid or, when the input of the next phase is
+// small, on the one CTA that took the decision ("solo"): it runs that phase
+// and the following small ones with block-level syncs, and releases the other
+// CTAs (which wait at the grid barrier) only when a phase is large again or
+// the run ends.  High-diameter graphs and the long tail of small buckets of
+// R-MAT are thousands of phases of a few hundred vertices; a block-level sync
+// costs far less than a grid barrier plus the dependent round trips of a
+// grid-wide decision.
+#pragma once
+
+#include "gbs_sssp_kernel.cuh"
+
+namespace gbs {
+
+// Who executes a phase: the whole grid or one CTA.
+struct Exec {
+    uint32_t tid, nthreads;   // thread index and count over the executors
+    uint32_t warp, nwarps;    // warp index and count over the executors
+};
+
+__device__ __forceinline__ Exec grid_exec() {
+    Exec x;
+    x.tid = blockIdx.x * blockDim.x + threadIdx.x;
+    x.nthreads = gridDim.x * blockDim.x;
+    x.warp = x.tid >> 5;
+    x.nwarps = x.nthreads >> 5;
+    return x;
+}
+
+__device__ __forceinline__ Exec cta_exec() {
+    Exec x;
+    x.tid = threadIdx.x;
+    x.nthreads = blockDim.x;
+    x.warp = x.tid >> 5;
+    x.nwarps = x.nthreads >> 5;
+    return x;
+}
+
+// ------------------------------------------------------------------- SCAN
+// One thread per frontier entry.  vtag != kTagInit keeps only entries whose
+// tag equals it (ring lists may hold entries that moved to a lower bucket).
+template <bool F32>
+__device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x, const uint32_t *F,
+                              uint32_t count, uint32_t vtag, bool light, bool add_s, uint32_t hround,
+                              uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    const uint32_t n = a.g.n;
+    Ctl *ctl = a.ws.ctl;
+    uint32_t my_edges = 0;
+    uint32_t nc = 0;   // candidates buffered by this warp
+    for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
+        const uint32_t i = base + lane;
+        uint32_t u = 0, du = 0, s = 0, e = 0;
+        bool ok = false;
+        if (i < count) {
+            u = __ldcg(F + i);
+            // the tag check and the row reads are independent: issue together
+            const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
+            du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
+            const uint32_t md = __ldg(a.ws.mid + u);
+            const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
+            ok = tg == vtag;
+            s = ok ? (light ? r : md) : 0u;
+            e = ok ? (light ? md : r) : 0u;
+        }
+        // S membership is decided now; the append waits until after the
+        // relaxation below so its latency overlaps that work
+        uint32_t hold = hround;
+        if (ok && add_s) hold = atomicExch(a.ws.hst + u, hround);
+        const uint32_t len = e - s;
+        // long rows -> descriptors, reserved with one atomic per warp
+        const uint32_t nd = len > kInlineEdges ? (len + kDescEdges - 1) / kDescEdges : 0u;
+        uint32_t incl = nd;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if (total) {
+            uint32_t dbase = 0;
+            if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt.v, total);
+            dbase = __shfl_sync(FULL, dbase, 31);
+            const uint32_t pos = dbase + incl - nd;
+            if (pos + nd <= a.ws.desc_cap) {
+                for (uint32_t c = 0; c < nd; ++c) {
+                    const uint32_t cs = s + c * kDescEdges;
+                    a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
+                }
+            } else if (nd) {
+                atomicExch(&ctl->error, (uint32_t)kErrCapacity);
+            }
+            my_edges += nd ? len : 0u;
+        }
+        // short rows: relaxed by this warp now
+        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, nc, imp);
+        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n,
+                    ok && add_s && hold != hround, u, ctl);
+    }
+    cand_drain<F32>(a, t, nc, imp);
+    // edges handed to EDGES (statistics / trace)
+    for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
+    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
+}
+
+// ------------------------------------------------------------------ EDGES
+// One warp per descriptor (<= kDescEdges edges of one row = one round).
+template <bool F32>
+__device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exec &x, uint32_t count,
+                                  uint32_t &imp) {
+    const unsigned lane = lane_id();
+    uint32_t nc = 0;   // candidates buffered by this warp
+    for (uint32_t c = x.warp; c < count; c += x.nwarps) {
+        const uint4 d = __ldcg(a.ws.desc + c);
+        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+        bool val[kUnroll];
+#pragma unroll
+        for (int j = 0; j < kUnroll; ++j) {
+            const uint32_t e = d.z + 32u * j + lane;
+            val[j] = e < d.w;
+            uo[j] = d.x;
+            duo[j] = d.y;
+            v[j] = 0;
+            w[j] = 0;
+            if (val[j]) {
+                const uint2 ew = ld_stream(a.g.adj + e);
+                v[j] = ew.x;
+                w[j] = ew.y;
+            }
+        }
+        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
+    }
+    cand_drain<F32>(a, t, nc, imp);
+}
+
+// Moves pending vertices whose bucket entered the window [W, W+kNB) into the
+// ring; the rest go to the other pending list.
+template <bool F32>
+__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr) {
+    const uint32_t n = a.g.n;
+    Ctl *ctl = a.ws.ctl;
+    const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
+    const uint32_t *list = a.ws.pend + (size_t)U.pend_sel * n;
+    Targets t;
+    t.cur_hi = 0;
+    t.W = U.W;
+    t.stamp_next = 0;
+    t.fq_next = 0;
+    t.pend_sel = U.pend_sel ^ 1u;
+    t.scr = scr;
+    for (uint32_t base = x.tid - lane_id(); base < count; base += x.nthreads) {
+        const uint32_t i = base + lane_id();
+        int q[1] = {-1};
+        uint32_t v[1] = {0};
+        if (i < count) {
+            v[0] = __ldcg(list + i);
+            if (__ldcg(a.ws.tag + v[0]) == kTagPending) {
+                const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v[0]) >> 32), a);
+                if ((unsigned long long)nb < (unsigned long long)U.W + kNB) {
+                    a.ws.tag[v[0]] = nb;
+                    q[0] = 1 + (int)(nb % kNB);
+                } else {
+                    atomicMin(&ctl->pend_min[t.pend_sel].v, nb);
+                    q[0] = kNB + 1;
+                }
+            }
+        }
+        warp_enqueue<1>(a, t, q, v);
+    }
+}
+
+// Runs the phase U.phase with executor x (grid or one CTA).
+template <bool F32>
+__device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
+                          uint32_t &imp) {
+    Ctl *ctl = a.ws.ctl;
+    const uint32_t n = a.g.n;
+    Targets t;
+    t.cur_hi = U.b + 1;
+    t.W = U.W;
+    t.stamp_next = U.epoch + 1;
+    t.fq_next = (U.epoch + 1) % 3u;
+    t.pend_sel = U.pend_sel;
+    t.scr = scr;
+    switch (U.phase) {
+        case kPhLightFirst:
+            scan_frontier<F32>(a, t, x, a.ws.ring + (size_t)(U.b % kNB) * n,
+                               min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), n), U.b, true, true, U.hround, imp);
+            break;
+        case kPhLight:
+            scan_frontier<F32>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
+                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, true, U.hround,
+                               imp);
+            break;
+        case kPhHeavy:
+            scan_frontier<F32>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
+                               min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), n), kTagInit, false, false, U.hround,
+                               imp);
+            break;
+        case kPhEdges:
+            relax_descriptors<F32>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
+            break;
+        case kPhPending:
+            rebucket_pending<F32>(a, U, x, scr);
+            break;
+        default:
+            break;
+    }
+}
+
+__device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
+    return phase == kPhHeavy ? (uint32_t)kPhHeavy : (uint32_t)kPhLight;
+}
+
+// The uniform state after the decision (identical in every CTA that adopts it).
+__device__ __forceinline__ Uniform advance_uniform(const Uniform &U, uint32_t next, uint32_t nb) {
+    Uniform N = U;
+    if (U.phase == kPhPending) {
+        N.pend_sel ^= 1u;
+    } else if (next == kPhEdges) {
+        N.logical = scan_kind(U.phase);
+    } else {
+        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
+        N.epoch += 1;
+        if (logical == kPhHeavy) N.hround += 1;
+    }
+    if (next == kPhLightFirst) { N.b = nb; N.W = nb; }
+    if (next == kPhPending) N.W = nb;
+    N.phase = next;
+    return N;
+}
+
+// Run by warp 0 of the deciding CTA after a phase: every other CTA has
+// finished it (or is waiting while this CTA runs alone), so all counters are
+// at rest.  Decides the next phase, resets the lists it appends to, records
+// statistics and the trace, publishes the new state and says whether the next
+// phase is small enough for this CTA to run alone.
+__device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool was_solo, bool &solo) {
+    Ctl *ctl = a.ws.ctl;
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    // one round trip: every counter the decision needs is loaded at once
+    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane].v);
+    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32].v);
+    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt.v);
+    const uint32_t edge_cnt = ld_relaxed(&ctl->edge_cnt.v);
+    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u].v);
+    const uint32_t fq_cur = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u].v);
+    const uint32_t s_cur = ld_relaxed(&ctl->s_cnt[U.hround & 1u].v);
+    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0].v), pc1 = ld_relaxed(&ctl->pend_cnt[1].v);
+    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0].v), pm1 = ld_relaxed(&ctl->pend_min[1].v);
+    const uint32_t err = ld_relaxed(&ctl->error);
+    auto ring_count = [&](uint32_t bucket) {
+        const uint32_t slot = bucket % kNB;
+        const uint32_t lo = __shfl_sync(FULL, ring_lo, slot & 31u);
+        const uint32_t hi = __shfl_sync(FULL, ring_hi, slot & 31u);
+        return slot < 32 ? lo : hi;
+    };
+    const uint32_t cur_ring = ring_count(U.b);
+
+    uint32_t next = kPhDone, nb = 0;
+    uint32_t ps2 = U.pend_sel;
+    bool need_ring_scan = false;
+    bool bucket_end = false;
+    uint32_t scan_from = 0;
+    if (U.phase == kPhPending) {
+        ps2 ^= 1u;
+        need_ring_scan = true;
+        scan_from = U.W;
+    } else if (U.phase != kPhEdges && desc_cnt > 0) {
+        next = kPhEdges;
+    } else {
+        const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
+        if (fq_next > 0) {
+            next = kPhLight;
+        } else if (logical == kPhLight) {
+            next = kPhHeavy;
+        } else {
+            bucket_end = true;
+            need_ring_scan = true;
+            scan_from = U.b + 1;
+        }
+    }
+    if (need_ring_scan) {
+        // first non-empty ring bucket in [scan_from, W + kNB); at a bucket end
+        // scan_from = b + 1 = W + 1, so the slot being cleared is not read.
+        const uint32_t lim = U.W + kNB;   // exclusive
+        uint32_t found = 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t off = 0; off < (uint32_t)kNB; off += 32u) {
+            const uint32_t bk = scan_from + off + lane;
+            const uint32_t c = ring_count(bk);
+            const unsigned m = __ballot_sync(FULL, bk < lim && c > 0);
+            if (m && found == 0xFFFFFFFFu) found = scan_from + off + (uint32_t)(__ffs(m) - 1);
+        }
+        const uint32_t pcnt = ps2 ? pc1 : pc0;
+        const uint32_t pm = ps2 ? pm1 : pm0;
+        if (pcnt > 0 && pm <= found) {
+            next = kPhPending;
+            nb = pm;
+        } else if (found != 0xFFFFFFFFu) {
+            next = kPhLightFirst;
+            nb = found;
+        } else {
+            next = kPhDone;
+        }
+    }
+    // whole-run limit: a run that has not finished within run_ns is stopped
+    if (globaltimer() - U.t0 > a.run_ns) {
+        next = kPhDone;
+        if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
+    }
+    if (err) next = kPhDone;
+    const Uniform N = advance_uniform(U, next, nb);
+    // size of the next phase's input
+    uint32_t items = 0;
+    switch (next) {
+        case kPhLightFirst: items = ring_count(nb); break;
+        case kPhLight: items = fq_next; break;
+        case kPhHeavy: items = s_cur; break;
+        case kPhEdges: items = desc_cnt; break;
+        case kPhPending: items = ps2 ? pc1 : pc0; break;
+        default: break;
+    }
+    solo = next != kPhDone && (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
+    if (lane == 0) {
+        if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
+            const uint32_t ti = ctl->trace_n;
+            if (ti < a.ws.trace_cap) {
+                uint32_t done_items;
+                switch (U.phase) {
+                    case kPhLightFirst: done_items = cur_ring; break;
+                    case kPhLight: done_items = fq_cur; break;
+                    case kPhHeavy: done_items = s_cur; break;
+                    case kPhEdges: done_items = desc_cnt; break;
+                    default: done_items = U.pend_sel ? pc1 : pc0; break;
+                }
+                TraceRec r;
+                r.kind = U.phase | (was_solo ? 16u : 0u);
+                r.bucket = U.b;
+                r.items = done_items;
+                r.edges = edge_cnt;
+                r.end_ns = globaltimer() - U.t0;
+                a.ws.trace[ti] = r;
+            }
+            ctl->trace_n = ti + 1;
+        }
+        ctl->st_phases += 1;
+        if (U.phase == kPhLightFirst) ctl->st_buckets += 1;
+        if (U.phase == kPhPending) {
+            ctl->st_pending_scans += 1;
+            ctl->pend_cnt[U.pend_sel].v = 0;          // the list just re-bucketed
+            ctl->pend_min[U.pend_sel].v = kTagInit;
+        }
+        if (was_solo) ctl->st_solo_phases += 1;
+        if (bucket_end) ctl->ring_cnt[U.b % kNB].v = 0;
+        if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
+            ctl->fq_cnt[(N.epoch + 1u) % 3u].v = 0;
+            ctl->desc_cnt.v = 0;
+            ctl->edge_cnt.v = 0;
+            if (N.hround != U.hround || next == kPhLightFirst) ctl->s_cnt[N.hround & 1u].v = 0;
+        }
+        ctl->pub_phase = N.phase;
+        ctl->pub_logical = N.logical;
+        ctl->pub_b = N.b;
+        ctl->pub_W = N.W;
+        ctl->pub_epoch = N.epoch;
+        ctl->pub_hround = N.hround;
+        ctl->pub_pend_sel = N.pend_sel;
+    }
+    __syncwarp();
+}
+
+// Thread 0 copies the published state to shared memory; the caller syncs.
+__device__ __forceinline__ void fetch_published(Ctl *ctl, uint32_t *s_pub) {
+    const bool err = ld_relaxed(&ctl->error) != 0;
+    s_pub[0] = err ? (uint32_t)kPhDone : ld_relaxed(&ctl->pub_phase);
+    s_pub[1] = ld_relaxed(&ctl->pub_logical);
+    s_pub[2] = ld_relaxed(&ctl->pub_b);
+    s_pub[3] = ld_relaxed(&ctl->pub_W);
+    s_pub[4] = ld_relaxed(&ctl->pub_epoch);
+    s_pub[5] = ld_relaxed(&ctl->pub_hround);
+    s_pub[6] = ld_relaxed(&ctl->pub_pend_sel);
+}
+
+__device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &U) {
+    U.phase = s_pub[0];
+    U.logical = s_pub[1];
+    U.b = s_pub[2];
+    U.W = s_pub[3];
+    U.epoch = s_pub[4];
+    U.hround = s_pub[5];
+    U.pend_sel = s_pub[6];
+}
+
+// Grid barrier after a phase.  The CTA that arrives last decides the next
+// phase (control_step); while the next phase is small it runs it alone and
+// decides again, and only then releases the waiting CTAs, which adopt the
+// published state.  Every wait is bounded by a.wait_ns (globaltimer); on
+// expiry the error word is set and every CTA leaves at its next check.  A
+// solo stretch stops after a.wait_ns / 4 so the waiting CTAs never time out.
+template <bool F32>
+__device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U, WarpScratch *scr,
+                                                   uint32_t &imp) {
+    Ctl *ctl = a.ws.ctl;
+    __shared__ uint32_t s_flag[2];
+    __shared__ uint32_t s_pub[8];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
+        const bool stall = (a.flags & GBS_F_TEST_STALL) && U.gen == 0 && blockIdx.x == 0;
+        uint32_t last = 0;
+        if (!stall) {
+            __threadfence();
+            last = atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1u;
+            if (last) __threadfence();
+        }
+        s_flag[0] = last;
+    }
+    __syncthreads();
+    if (s_flag[0]) {
+        const unsigned long long ts = globaltimer();
+        bool was_solo = false;
+        for (;;) {
+            if (threadIdx.x < 32) {
+                bool solo = false;
+                control_step(a, U, was_solo, solo);
+                if (threadIdx.x == 0) {
+                    s_flag[1] = solo && (globaltimer() - ts) < a.wait_ns / 4;
+                    fetch_published(ctl, s_pub);
+                }
+            }
+            __syncthreads();
+            adopt_published(s_pub, U);
+            const bool solo = s_flag[1] != 0;
+            __syncthreads();
+            if (!solo) break;
+            run_phase<F32>(a, U, cta_exec(), scr, imp);
+            __syncthreads();
+            was_solo = true;
+        }
+        if (threadIdx.x == 0) {
+            ctl->bar_count = 0;
+            __threadfence();
+            st_release(&ctl->bar_gen, U.gen + 1u);
+        }
+    } else {
+        if (threadIdx.x == 0) {
+            const unsigned long long t0 = globaltimer();
+            uint32_t spins = 0;
+            while (ld_acquire(&ctl->bar_gen) != U.gen + 1u) {
+                if ((++spins & 255u) == 0) {
+                    if (ld_relaxed(&ctl->error) != 0) break;
+                    if (globaltimer() - t0 > a.wait_ns) {
+                        atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+            fetch_published(ctl, s_pub);
+        }
+        __syncthreads();
+        adopt_published(s_pub, U);
+    }
+    __syncthreads();
+    U.gen += 1;
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
+    Ctl *ctl = a.ws.ctl;
+    __shared__ WarpScratch s_scr[kTPB / 32];
+    WarpScratch *scr = &s_scr[threadIdx.x >> 5];
+    Uniform U;
+    U.phase = ld_relaxed(&ctl->pub_phase);
+    U.logical = kPhLight;
+    U.b = ld_relaxed(&ctl->pub_b);
+    U.W = U.b;
+    U.epoch = a.epoch0;
+    U.hround = a.hround0;
+    U.pend_sel = 0;
+    U.gen = 0;
+    U.t0 = globaltimer();
+    uint32_t imp = 0;
+    while (U.phase != kPhDone) {
+        run_phase<F32>(a, U, grid_exec(), scr, imp);
+        barrier_and_decide<F32>(a, U, scr, imp);
+    }
+    for (int o = 16; o > 0; o >>= 1) imp += __shfl_down_sync(0xffffffffu, imp, o);
+    if (lane_id() == 0 && imp) atomicAdd(&ctl->st_improvements, (unsigned long long)imp);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->next_epoch = U.epoch;        // next free stamps for the following run
+        ctl->next_hround = U.hround;
+    }
+}
+
+}  // namespace gbs

@@ -68,11 +68,15 @@ typedef struct gbs_params {
     uint32_t flags;          /* GBS_F_* */
     uint32_t wait_limit_ms;  /* device-side wait limit; 0 = 4000 ms (a whole run
                                 is limited to 16 times this) */
-    uint32_t reserved[2];
+    uint32_t solo_entries;   /* a scan of at most this many frontier entries runs on
+                                one CTA without a grid barrier; 0 = 1024 */
+    uint32_t solo_descs;     /* likewise for a relaxation of at most this many
+                                128-edge descriptors; 0 = 64 */
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
 #define GBS_F_TRACE 0x2u     /* record one gbs_phase_rec per grid phase (gbs_trace) */
+#define GBS_F_NO_SOLO 0x4u   /* run every phase on the whole grid */
 /* Failure-path test: one CTA never arrives at the first grid barrier, so every
  * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
  * wait_limit_ms and the device stays usable.  Never set in normal use. */
@@ -90,6 +94,8 @@ typedef struct gbs_stats {
     uint32_t blocks;         /* CTAs of the persistent launch */
     double delta_used;       /* bucket width actually used */
     double light_used;       /* light/heavy split actually used */
+    uint32_t solo_phases;    /* phases run by one CTA without a grid barrier */
+    uint32_t reserved;
 } gbs_stats;
 
 /* Library / device */
@@ -150,7 +156,8 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
 /*
  * Per-phase record of the last run made with GBS_F_TRACE (the GPU analogue
  * of the reference's per-phase rdtsc slots and bucket dumps,
- * sssp/csr_sspath_array.c:1121-1170).  kind: 0 scan of a new bucket, 1 scan
+ * sssp/csr_sspath_array.c:1121-1170).  kind (low 4 bits; +16 if the phase ran
+ * on one CTA without a grid barrier): 0 scan of a new bucket, 1 scan
  * of a repeated light frontier, 2 scan of the settled list for heavy edges,
  * 3 edge relaxation, 4 pending re-bucketing.  items: frontier entries
  * (scans), edge descriptors (relaxation) or pending entries; edges: edges

@@ -99,6 +99,26 @@ def test_hub_rows_split_into_descriptors(gb, orc):
     run_and_check(gb, orc, a.row, a.col, a.w, src, delta=100000)
 
 
+@pytest.mark.parametrize("mode", ["grid_only", "default", "all_solo"])
+def test_solo_phases_same_result(mode, gb, orc):
+    """Phases run by one CTA (small inputs) or by the whole grid give the same
+    result; 'all_solo' makes every phase after the first run on one CTA."""
+    kw = {"grid_only": dict(flags=gb.F_NO_SOLO),
+          "default": {},
+          "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30)}[mode]
+    a = gb.gen_rmat(13, 16, 11)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, **kw)
+    if mode == "grid_only":
+        assert st["solo_phases"] == 0
+    if mode == "all_solo":
+        assert st["solo_phases"] >= st["phases"] - 2
+    g2 = gb.gen_grid(64, 96, 5, "f32")
+    _, _, st2 = run_and_check(gb, orc, g2.row, g2.col, g2.w, 0, **kw)
+    if mode == "default":
+        assert st2["solo_phases"] > 0
+
+
 def test_phase_trace(gb, orc):
     """GBS_F_TRACE records one entry per grid phase; scans are followed by a
     relaxation of the edges they emitted, and device time is monotone."""
