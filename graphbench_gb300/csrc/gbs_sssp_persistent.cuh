@@ -443,6 +443,11 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             __syncthreads();
             if (!solo) break;
             run_phase<F32>(a, U, cta_exec(), scr, imp);
+            // atomics whose result is unused (tag and pend_min minima) are
+            // fire-and-forget reductions; each thread waits until its own have
+            // reached L2 before the decision reads the counters and tags they
+            // feed (the grid path gets this from the fence before arrival)
+            __threadfence();
             __syncthreads();
             was_solo = true;
         }
