@@ -56,7 +56,8 @@ class Params(ctypes.Structure):
 
 class PhaseRec(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_uint32), ("bucket", ctypes.c_uint32), ("items", ctypes.c_uint32),
-                ("edges", ctypes.c_uint32), ("end_ns", ctypes.c_uint64)]
+                ("edges", ctypes.c_uint32), ("pending", ctypes.c_uint32), ("window", ctypes.c_uint32),
+                ("end_ns", ctypes.c_uint64)]
 
 
 PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "scan_heavy", 3: "relax", 4: "pending"}
@@ -321,7 +322,8 @@ class Graph:
         recs = (PhaseRec * max(1, cnt.value))()
         _check(lib.gbs_trace(self._h, recs, cnt.value, ctypes.byref(cnt)), "gbs_trace")
         return [{"kind": PHASE_KINDS.get(r.kind & 15, r.kind), "solo": bool(r.kind & 16),
-                 "bucket": r.bucket, "items": r.items, "edges": r.edges, "end_ns": r.end_ns}
+                 "bucket": r.bucket, "items": r.items, "edges": r.edges, "pending": r.pending,
+                 "window": r.window, "end_ns": r.end_ns}
                 for r in recs[: cnt.value]]
 
     def sssp(self, source: int, delta: float | None = None, light: float | None = None,

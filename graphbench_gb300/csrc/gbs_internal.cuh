@@ -49,6 +49,8 @@ struct TraceRec {
     uint32_t bucket;
     uint32_t items;
     uint32_t edges;
+    uint32_t pending;       // entries of the live pending list after the phase
+    uint32_t window;        // ring window base during the phase
     unsigned long long end_ns;
 };
 

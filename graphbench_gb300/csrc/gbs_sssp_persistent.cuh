@@ -155,13 +155,16 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     t.fq_next = 0;
     t.pend_sel = U.pend_sel ^ 1u;
     t.scr = scr;
+    uint32_t stale = 0;
     for (uint32_t base = x.tid - lane_id(); base < count; base += x.nthreads) {
         const uint32_t i = base + lane_id();
         int q[1] = {-1};
         uint32_t v[1] = {0};
         if (i < count) {
             v[0] = __ldcg(list + i);
-            if (__ldcg(a.ws.tag + v[0]) == kTagPending) {
+            const uint32_t tg = __ldcg(a.ws.tag + v[0]);
+            stale += tg != kTagPending ? 1u : 0u;
+            if (tg == kTagPending) {
                 const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v[0]) >> 32), a);
                 if ((unsigned long long)nb < (unsigned long long)U.W + kNB) {
                     a.ws.tag[v[0]] = nb;
@@ -174,6 +177,9 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
         }
         warp_enqueue<1>(a, t, q, v);
     }
+    // entries that had already left the pending list (statistics / trace)
+    for (int o = 16; o > 0; o >>= 1) stale += __shfl_down_sync(0xffffffffu, stale, o);
+    if (lane_id() == 0 && stale) atomicAdd(&ctl->edge_cnt.v, stale);
 }
 
 // Runs the phase U.phase with executor x (grid or one CTA).
@@ -329,7 +335,10 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         case kPhPending: items = ps2 ? pc1 : pc0; break;
         default: break;
     }
-    solo = next != kPhDone && (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
+    // re-bucketing always runs on the grid: run on one CTA it lost survivors
+    // (measured; cause not yet understood), and it happens a few times per run
+    solo = next != kPhDone && next != kPhPending &&
+           (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
     if (lane == 0) {
         if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
             const uint32_t ti = ctl->trace_n;
@@ -347,6 +356,8 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
                 r.bucket = U.b;
                 r.items = done_items;
                 r.edges = edge_cnt;
+                r.pending = N.pend_sel ? pc1 : pc0;
+                r.window = U.W;
                 r.end_ns = globaltimer() - U.t0;
                 a.ws.trace[ti] = r;
             }
@@ -360,6 +371,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             ctl->pend_min[U.pend_sel].v = kTagInit;
         }
         if (was_solo) ctl->st_solo_phases += 1;
+        if (next == kPhPending) ctl->edge_cnt.v = 0;   // counts stale entries there
         if (bucket_end) ctl->ring_cnt[U.b % kNB].v = 0;
         if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
             ctl->fq_cnt[(N.epoch + 1u) % 3u].v = 0;

@@ -159,7 +159,8 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
  * sssp/csr_sspath_array.c:1121-1170).  kind (low 4 bits; +16 if the phase ran
  * on one CTA without a grid barrier): 0 scan of a new bucket, 1 scan
  * of a repeated light frontier, 2 scan of the settled list for heavy edges,
- * 3 edge relaxation, 4 pending re-bucketing.  items: frontier entries
+ * 3 edge relaxation, 4 pending re-bucketing (its edges field counts entries
+ * that had already left the pending list).  items: frontier entries
  * (scans), edge descriptors (relaxation) or pending entries; edges: edges
  * the scan handed to the relaxation; end_ns: device time since kernel start.
  * *count receives the number of records (may exceed cap).
@@ -169,6 +170,8 @@ typedef struct gbs_phase_rec {
     uint32_t bucket;
     uint32_t items;
     uint32_t edges;
+    uint32_t pending;        /* entries of the live pending list after the phase */
+    uint32_t window;         /* ring window base during the phase */
     uint64_t end_ns;
 } gbs_phase_rec;
 
