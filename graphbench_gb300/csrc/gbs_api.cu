@@ -293,6 +293,14 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     const bool no_solo = (a.flags & GBS_F_NO_SOLO) != 0;
     a.solo_items = no_solo ? 0u : ((p && p->solo_entries) ? p->solo_entries : 1024u);
     a.solo_desc = no_solo ? 0u : ((p && p->solo_descs) ? p->solo_descs : 64u);
+    uint32_t max_bits;
+    if (g->wtype == GBS_WEIGHT_U32) {
+        max_bits = (uint32_t)g->max_w;
+    } else {
+        const float mf = (float)g->max_w;
+        std::memcpy(&max_bits, &mf, 4);
+    }
+    a.no_heavy = r.light_bits >= max_bits ? 1u : 0u;
     a.run_ns = a.wait_ns * 16ull;
     if (a.flags & GBS_F_TRACE) {
         if (!g->ws.trace) {

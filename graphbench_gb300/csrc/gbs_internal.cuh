@@ -131,6 +131,7 @@ struct SsspArgs {
     uint32_t flags;         // GBS_F_* of the call
     uint32_t solo_items;    // a SCAN/PENDING phase with at most this many entries runs on one CTA
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
+    uint32_t no_heavy;      // the split covers every edge: light scans relax whole rows, no HEAVY phase
     unsigned long long wait_ns;   // limit of one barrier wait
     unsigned long long run_ns;    // limit of the whole run
 };

@@ -198,12 +198,13 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     switch (U.phase) {
         case kPhLightFirst:
             scan_frontier<F32>(a, t, x, a.ws.ring + (size_t)(U.b % kNB) * n,
-                               min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), n), U.b, true, true, U.hround, imp);
+                               min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), n), U.b, true, !a.no_heavy, U.hround,
+                               imp);
             break;
         case kPhLight:
             scan_frontier<F32>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, true, U.hround,
-                               imp);
+                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, !a.no_heavy,
+                               U.hround, imp);
             break;
         case kPhHeavy:
             scan_frontier<F32>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
@@ -286,7 +287,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
         if (fq_next > 0) {
             next = kPhLight;
-        } else if (logical == kPhLight) {
+        } else if (logical == kPhLight && !a.no_heavy) {
             next = kPhHeavy;
         } else {
             bucket_end = true;

@@ -139,6 +139,24 @@ def test_phase_trace(gb, orc):
     assert np.array_equal(d, d2) and np.array_equal(d, orc.dijkstra(a.row, a.col, a.w, src))
 
 
+@pytest.mark.parametrize("wtype", ["u32", "f32"])
+def test_split_covering_all_edges_skips_heavy(wtype, gb, orc):
+    """A light bound at or above the largest weight leaves no heavy edge: the
+    light scans relax whole rows and no heavy scan runs; a bound just below
+    the largest weight keeps the heavy scans."""
+    a = gb.gen_rmat(12, 16, 21, wtype)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    wmax = float(a.w.max())
+    with gb.Graph.from_host(a) as g:
+        for light, heavy_expected in [(wmax, False), (wmax * 4, False), (wmax - 1, True)]:
+            d, p, st = g.sssp(src, delta=wmax / 8, light=light, flags=gb.F_TRACE)
+            kinds = {r["kind"] for r in g.trace()}
+            assert ("scan_heavy" in kinds) == heavy_expected, (light, kinds)
+            ref = orc.dijkstra(a.row, a.col, a.w, src)
+            assert np.array_equal(d, ref)
+            assert np.array_equal(p, orc.min_tight_pred(a.row, a.col, a.w, src, ref))
+
+
 def test_pending_list_small_delta(gb, orc):
     """delta = 1 with weights up to 255 pushes vertices past the 64-bucket
     ring window, exercising the pending list and its re-bucketing."""
