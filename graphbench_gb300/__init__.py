@@ -35,8 +35,10 @@ EXPORTS = [
     "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
     "gbs_sssp_multi", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
+    "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
+    "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
     "gbs_device_alloc", "gbs_device_free",
-    "gbs_device_synchronize",
+    "gbs_device_synchronize", "gbs_memcpy",
     "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
 ]
 
@@ -79,6 +81,36 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CsrView(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("m", ctypes.c_uint64), ("row_offsets", ctypes.c_void_p),
+                ("cols", ctypes.c_void_p), ("weights", ctypes.c_void_p)]
+
+
+class BatchParams(ctypes.Structure):
+    _fields_ = [("delta", ctypes.c_double), ("delta_scale", ctypes.c_double), ("light", ctypes.c_double),
+                ("group_ctas", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("wait_limit_ms", ctypes.c_uint32), ("solo_entries", ctypes.c_uint32),
+                ("solo_descs", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class InstStats(ctypes.Structure):
+    _fields_ = [("done", ctypes.c_uint32), ("error", ctypes.c_uint32), ("group", ctypes.c_uint32),
+                ("phases", ctypes.c_uint32), ("buckets", ctypes.c_uint32), ("pending_scans", ctypes.c_uint32),
+                ("solo_phases", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("reached", ctypes.c_uint64),
+                ("edges_reached", ctypes.c_uint64), ("improvements", ctypes.c_uint64),
+                ("start_ns", ctypes.c_uint64), ("end_ns", ctypes.c_uint64)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("instances", ctypes.c_uint32), ("completed", ctypes.c_uint32),
+                ("groups", ctypes.c_uint32), ("group_ctas", ctypes.c_uint32), ("blocks", ctypes.c_uint32),
+                ("max_phases", ctypes.c_uint32), ("phases", ctypes.c_uint64), ("reached", ctypes.c_uint64),
+                ("edges_reached", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class HostCsr(ctypes.Structure):
     _fields_ = [("n", ctypes.c_uint32), ("m", ctypes.c_uint64),
                 ("row_offsets", ctypes.POINTER(ctypes.c_uint64)),
@@ -106,6 +138,7 @@ def _load() -> ctypes.CDLL:
     L.gbs_host_free.argtypes = [P]
     L.gbs_device_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
     L.gbs_device_free.argtypes = [P]
+    L.gbs_memcpy.argtypes = [P, P, ctypes.c_size_t]
     L.gbs_gen_rmat.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
                                ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.POINTER(HostCsr))]
     L.gbs_gen_grid.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
@@ -116,6 +149,15 @@ def _load() -> ctypes.CDLL:
     # no-allocation variant: device pointers in, device pointers out
     L.gbs_sssp_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_uint64, P, P, ctypes.c_int, ctypes.c_uint32,
                                    ctypes.c_double, P, P, P]
+    # batched launches
+    L.gbs_pack_create.argtypes = [ctypes.c_uint32, P, ctypes.c_int, ctypes.POINTER(P)]
+    L.gbs_pack_destroy.argtypes = [P]
+    L.gbs_pack_info.argtypes = [P, P, P, P, P]
+    L.gbs_plan_sources.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(BatchParams), P, P, ctypes.POINTER(P)]
+    L.gbs_plan_pack.argtypes = [P, P, ctypes.POINTER(BatchParams), P, P, ctypes.POINTER(P)]
+    L.gbs_plan_launch.argtypes = [P]
+    L.gbs_plan_wait.argtypes = [P, ctypes.POINTER(BatchStats), P]
+    L.gbs_plan_destroy.argtypes = [P]
     return L
 
 
@@ -409,3 +451,150 @@ def run_sspath_arr(gs: TCsr, source: int, delta: float) -> np.ndarray:
         out[dist == np.uint32(0xFFFFFFFF)] = math.inf
     gs.weight = out
     return out
+
+
+# --------------------------------------------------------------- batched
+def batch_params(delta: float | None = None, delta_scale: float | None = None, light: float | None = None,
+                 group_ctas: int = 0, flags: int = 0, wait_limit_ms: int = 0, solo_entries: int = 0,
+                 solo_descs: int = 0) -> BatchParams:
+    """light=None: light bound = delta; light=math.inf: no light/heavy split."""
+    p = BatchParams()
+    p.delta = float(delta) if delta else 0.0
+    p.delta_scale = float(delta_scale) if delta_scale else 0.0
+    p.light = float(light) if light is not None else -1.0
+    p.group_ctas = group_ctas
+    p.flags = flags
+    p.wait_limit_ms = wait_limit_ms
+    p.solo_entries = solo_entries
+    p.solo_descs = solo_descs
+    return p
+
+
+class Pack:
+    """Independent graphs uploaded together (gbs_pack) for batched SSSP."""
+
+    def __init__(self, graphs: list[HostGraph]):
+        if not graphs:
+            raise ValueError("empty pack")
+        dt = graphs[0].w.dtype
+        if any(g.w.dtype != dt for g in graphs):
+            raise TypeError("every graph of a pack has the same weight type")
+        self.wtype = W_F32 if dt == np.float32 else W_U32
+        self.dist_dtype = np.float32 if self.wtype == W_F32 else np.uint32
+        self._keep = [(np.ascontiguousarray(g.row, dtype=np.uint64), np.ascontiguousarray(g.col, dtype=np.uint32),
+                       np.ascontiguousarray(g.w)) for g in graphs]
+        views = (CsrView * len(graphs))()
+        for i, (r, c, w) in enumerate(self._keep):
+            views[i] = CsrView(len(r) - 1, len(c), r.ctypes.data, c.ctypes.data, w.ctypes.data)
+        h = ctypes.c_void_p()
+        _check(lib.gbs_pack_create(len(graphs), views, self.wtype, ctypes.byref(h)), "gbs_pack_create")
+        self._h = h
+        self._keep = None
+        cnt, tn, tm = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64()
+        offs = np.zeros(len(graphs) + 1, dtype=np.uint64)
+        _check(lib.gbs_pack_info(h, ctypes.byref(cnt), ctypes.byref(tn), ctypes.byref(tm), _ptr(offs)),
+               "gbs_pack_info")
+        self.count, self.total_n, self.total_m = cnt.value, tn.value, tm.value
+        self.vertex_offsets = offs
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.gbs_pack_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Plan:
+    """A batched launch captured in a CUDA graph (gbs_plan).  Outputs stay in
+    device memory owned by the plan object: dist (and pred) hold every
+    instance's arrays back to back."""
+
+    def __init__(self, target, sources, params: BatchParams | None = None, want_pred: bool = True, **kw):
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        params = params if params is not None else batch_params(**kw)
+        if isinstance(target, Graph):
+            self.k, n = len(src), target.n
+            self.offsets = np.arange(self.k + 1, dtype=np.uint64) * np.uint64(n)
+            self.dist_dtype = target.dist_dtype
+        elif isinstance(target, Pack):
+            if len(src) != target.count:
+                raise ValueError("one source per pack graph")
+            self.k = target.count
+            self.offsets = target.vertex_offsets.copy()
+            self.dist_dtype = target.dist_dtype
+        else:
+            raise TypeError("target must be a Graph or a Pack")
+        total = int(self.offsets[-1])
+        self.dist = DeviceBuffer(max(4, 4 * total))
+        self.pred = DeviceBuffer(max(4, 4 * total)) if want_pred else None
+        h = ctypes.c_void_p()
+        pp = self.pred.ptr if self.pred else None
+        if isinstance(target, Graph):
+            _check(lib.gbs_plan_sources(target.handle, _ptr(src), self.k, ctypes.byref(params), self.dist.ptr, pp,
+                                        ctypes.byref(h)), "gbs_plan_sources")
+        else:
+            _check(lib.gbs_plan_pack(target._h, _ptr(src), ctypes.byref(params), self.dist.ptr, pp,
+                                     ctypes.byref(h)), "gbs_plan_pack")
+        self._h = h
+        self.target = target
+
+    def launch(self) -> None:
+        _check(lib.gbs_plan_launch(self._h), "gbs_plan_launch")
+
+    def wait(self, per_instance: bool = False):
+        st = BatchStats()
+        inst = (InstStats * self.k)() if per_instance else None
+        _check(lib.gbs_plan_wait(self._h, ctypes.byref(st), inst), "gbs_plan_wait")
+        d = st.as_dict()
+        if per_instance:
+            d["per_instance"] = [{k: getattr(r, k) for k, _ in InstStats._fields_} for r in inst]
+        return d
+
+    def run(self, per_instance: bool = False):
+        self.launch()
+        return self.wait(per_instance)
+
+    def results(self, want_pred: bool = True):
+        """Copies the outputs to the host: lists of per-instance arrays."""
+        total = int(self.offsets[-1])
+        dist = np.empty(total, dtype=self.dist_dtype)
+        _check(lib.gbs_memcpy(_ptr(dist), self.dist.ptr, 4 * total), "gbs_memcpy")
+        pred = None
+        if want_pred and self.pred is not None:
+            pred = np.empty(total, dtype=np.int32)
+            _check(lib.gbs_memcpy(_ptr(pred), self.pred.ptr, 4 * total), "gbs_memcpy")
+        o = [int(x) for x in self.offsets]
+        ds = [dist[o[i]:o[i + 1]] for i in range(self.k)]
+        ps = [pred[o[i]:o[i + 1]] for i in range(self.k)] if pred is not None else None
+        return ds, ps
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.gbs_plan_destroy(self._h)
+            self._h = None
+        for b in (getattr(self, "dist", None), getattr(self, "pred", None)):
+            if b is not None:
+                b.free()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -20,7 +20,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libgbsssp.so"
 
-CUDA_SOURCES = ["csrc/gbs_api.cu", "csrc/gbs_noalloc.cu"]
+CUDA_SOURCES = ["csrc/gbs_api.cu", "csrc/gbs_batch.cu", "csrc/gbs_noalloc.cu"]
 C_SOURCES = ["host/gen.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -17,7 +17,7 @@
 #include <thread>
 #include <vector>
 
-#include "gbs_sssp_persistent.cuh"
+#include "gbs_host.hpp"
 
 using namespace gbs;
 
@@ -25,24 +25,11 @@ namespace {
 
 thread_local std::string g_last_error;
 
-gbs_status fail(gbs_status s, const std::string &msg) {
-    g_last_error = msg;
-    return s;
-}
-
 }  // namespace
 
 void gbs::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
 
 namespace {
-
-#define GBS_CUDA(call)                                                                       \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
-            return fail(e_ == cudaErrorMemoryAllocation ? GBS_ERR_NO_MEMORY : GBS_ERR_CUDA,  \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                 \
-    } while (0)
 
 // ------------------------------------------------------------------ kernels
 __global__ void k_mid(const uint32_t *__restrict__ row, const uint2 *__restrict__ adj, uint32_t n,
@@ -106,32 +93,7 @@ __global__ void k_stats(const unsigned long long *__restrict__ dp, const uint32_
 
 }  // namespace
 
-// ------------------------------------------------------------------- graph
-struct gbs_graph {
-    uint32_t n = 0;
-    uint64_t m = 0;
-    gbs_weight_type wtype = GBS_WEIGHT_U32;
-    double max_w = 0.0;
-    int device = 0;
-    int sms = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    uint32_t *d_row = nullptr;
-    uint2 *d_adj = nullptr;
-    // workspace
-    bool ws_ready = false;
-    Workspace ws{};
-    uint32_t *d_dist = nullptr;
-    int32_t *d_pred = nullptr;
-    uint32_t mid_light_bits = 0;
-    bool mid_valid = false;
-    uint32_t epoch = 1, hround = 1;
-    uint32_t trace_n = 0;
-    int blocks = 0;
-    Ctl host_ctl{};
-};
-
-namespace {
+namespace gbs {
 
 void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits, uint32_t n,
                std::vector<uint2> &adj) {
@@ -160,37 +122,105 @@ void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits,
     for (auto &t : th) t.join();
 }
 
-gbs_status ensure_workspace(gbs_graph *g) {
-    if (g->ws_ready) return GBS_OK;
-    const size_t n = g->n ? g->n : 1;
-    Workspace &w = g->ws;
+gbs_status prepare_csr(uint32_t n, uint64_t m, const uint64_t *row_offsets, const uint32_t *cols,
+                       const void *weights, gbs_weight_type wtype, std::vector<uint32_t> &row32,
+                       std::vector<uint2> &adj, double &max_w) {
+    if (!row_offsets || (m && (!cols || !weights)))
+        return fail(GBS_ERR_INVALID_ARG, "NULL CSR array");
+    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32)
+        return fail(GBS_ERR_INVALID_ARG, "unknown weight type");
+    if (n == 0 || n > 0x7FFFFFFFu) return fail(GBS_ERR_INVALID_ARG, "vertex count must be in [1, 2^31)");
+    if (m >= 0xFFFFFFFFull) return fail(GBS_ERR_UNSUPPORTED, "edge count must be < 2^32");
+    if (row_offsets[0] != 0 || row_offsets[n] != m)
+        return fail(GBS_ERR_INVALID_ARG, "row_offsets must start at 0 and end at m");
+    for (uint32_t v = 0; v < n; ++v)
+        if (row_offsets[v + 1] < row_offsets[v]) return fail(GBS_ERR_INVALID_ARG, "row_offsets decrease");
+    std::vector<uint32_t> wbits(m);
+    max_w = 0.0;
+    for (uint64_t e = 0; e < m; ++e) {
+        if (cols[e] >= n) return fail(GBS_ERR_INVALID_ARG, "column index out of range");
+        if (wtype == GBS_WEIGHT_U32) {
+            const uint32_t w = ((const uint32_t *)weights)[e];
+            wbits[e] = w;
+            if (w > max_w) max_w = w;
+        } else {
+            float w = ((const float *)weights)[e];
+            if (!(w >= 0.0f) || std::isinf(w))
+                return fail(GBS_ERR_INVALID_ARG, "float32 weights must be finite and >= 0");
+            if (w == 0.0f) w = 0.0f;  // -0.0 -> +0.0
+            std::memcpy(&wbits[e], &w, 4);
+            if (w > max_w) max_w = w;
+        }
+    }
+    adj.resize(m);
+    sort_rows(row_offsets, cols, wbits.data(), n, adj);
+    row32.resize((size_t)n + 1);
+    for (uint32_t v = 0; v <= n; ++v) row32[v] = (uint32_t)row_offsets[v];
+    return GBS_OK;
+}
+
+gbs_status alloc_workspace(Workspace &w, uint32_t n_cap, uint64_t m_cap, cudaStream_t s) {
+    const size_t n = n_cap ? n_cap : 1;
     GBS_CUDA(cudaMalloc(&w.dp, sizeof(unsigned long long) * n));
     GBS_CUDA(cudaMalloc(&w.tag, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&w.fst, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&w.hst, sizeof(uint32_t) * n));
-    GBS_CUDA(cudaMalloc(&w.mid, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&w.ring, sizeof(uint32_t) * n * kNB));
     GBS_CUDA(cudaMalloc(&w.fq, sizeof(uint32_t) * n * 3));
     GBS_CUDA(cudaMalloc(&w.S, sizeof(uint32_t) * n * 2));
     GBS_CUDA(cudaMalloc(&w.pend, sizeof(uint32_t) * n * 2));
     // a SCAN reads at most n entries and cuts each row into ceil(len/kDescEdges)
     // descriptors, so it emits at most n + m/kDescEdges of them
-    const uint64_t cap = (uint64_t)g->n + g->m / kDescEdges + 64;
+    const uint64_t cap = (uint64_t)n_cap + m_cap / kDescEdges + 64;
     w.desc_cap = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFF0ull);
     GBS_CUDA(cudaMalloc(&w.desc, sizeof(uint4) * (size_t)w.desc_cap));
-    w.trace = nullptr;
-    w.trace_cap = 0;
     GBS_CUDA(cudaMalloc(&w.ctl, sizeof(Ctl)));
+    GBS_CUDA(cudaMemsetAsync(w.fst, 0, sizeof(uint32_t) * n, s));
+    GBS_CUDA(cudaMemsetAsync(w.hst, 0, sizeof(uint32_t) * n, s));
+    GBS_CUDA(cudaMemsetAsync(w.ctl, 0, sizeof(Ctl), s));
+    w.n_cap = n_cap;
+    return GBS_OK;
+}
+
+void free_workspace(Workspace &w) {
+    cudaFree(w.dp); cudaFree(w.tag); cudaFree(w.fst); cudaFree(w.hst);
+    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.desc); cudaFree(w.ctl);
+    w = Workspace{};
+}
+
+int persistent_ctas_per_sm(bool f32, bool batch) {
+    const void *kfn = batch ? (f32 ? (const void *)sssp_batch<true> : (const void *)sssp_batch<false>)
+                            : (f32 ? (const void *)sssp_persistent<true> : (const void *)sssp_persistent<false>);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kTPB, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm;
+}
+
+gbs_status launch_mid(const uint32_t *row, const uint2 *adj, uint32_t n, uint32_t light_bits, uint32_t *mid,
+                      int sms, cudaStream_t s) {
+    const int tb = 256;
+    const int eb = std::max(1, std::min<int>((n + tb - 1) / tb, sms * 8));
+    k_mid<<<eb, tb, 0, s>>>(row, adj, n, light_bits, mid);
+    GBS_CUDA(cudaGetLastError());
+    return GBS_OK;
+}
+
+gbs_status ensure_workspace(gbs_graph *g) {
+    if (g->ws_ready) return GBS_OK;
+    const size_t n = g->n ? g->n : 1;
+    gbs_status st = alloc_workspace(g->ws, g->n, g->m, g->stream);
+    if (st != GBS_OK) return st;
+    GBS_CUDA(cudaMalloc(&g->ws.mid, sizeof(uint32_t) * n));
+    g->ws.trace = nullptr;
+    g->ws.trace_cap = 0;
     GBS_CUDA(cudaMalloc(&g->d_dist, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&g->d_pred, sizeof(int32_t) * n));
-    GBS_CUDA(cudaMemsetAsync(w.fst, 0, sizeof(uint32_t) * n, g->stream));
-    GBS_CUDA(cudaMemsetAsync(w.hst, 0, sizeof(uint32_t) * n, g->stream));
     g->epoch = 1;
     g->hround = 1;
-    int per_sm = 0;
-    const void *kfn = g->wtype == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<true>
-                                                 : (const void *)sssp_persistent<false>;
-    GBS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kTPB, 0));
+    const int per_sm = persistent_ctas_per_sm(g->wtype == GBS_WEIGHT_F32, false);
     if (per_sm < 1) return fail(GBS_ERR_UNSUPPORTED, "persistent kernel cannot be resident");
     g->blocks = per_sm * g->sms;
     g->ws_ready = true;
@@ -201,10 +231,9 @@ void free_graph(gbs_graph *g) {
     if (!g) return;
     cudaFree(g->d_row);
     cudaFree(g->d_adj);
-    Workspace &w = g->ws;
-    cudaFree(w.dp); cudaFree(w.tag); cudaFree(w.fst); cudaFree(w.hst); cudaFree(w.mid);
-    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.desc); cudaFree(w.ctl);
-    cudaFree(w.trace);
+    cudaFree(g->ws.mid);
+    cudaFree(g->ws.trace);
+    free_workspace(g->ws);
     cudaFree(g->d_dist);
     cudaFree(g->d_pred);
     for (auto &e : g->ev) if (e) cudaEventDestroy(e);
@@ -212,24 +241,26 @@ void free_graph(gbs_graph *g) {
     delete g;
 }
 
-struct Resolved {
-    double delta, light;
-    uint32_t delta_u, light_bits;
-    float inv_delta_f;
-};
-
-double default_delta(const gbs_graph *g) {
-    if (g->m == 0 || g->n == 0) return 1.0;
-    const double avg = (double)g->m / (double)g->n;
-    const double d = g->max_w / avg;
+double default_delta(double max_w, uint32_t n, uint64_t m) {
+    if (m == 0 || n == 0) return 1.0;
+    const double avg = (double)m / (double)n;
+    const double d = max_w / avg;
     return d > 0 ? d : 1.0;
 }
 
-Resolved resolve(const gbs_graph *g, const gbs_params *p) {
+uint32_t max_weight_bits(gbs_weight_type wt, double max_w) {
+    if (wt == GBS_WEIGHT_U32) return (uint32_t)max_w;
+    const float mf = (float)max_w;
+    uint32_t bits;
+    std::memcpy(&bits, &mf, 4);
+    return bits;
+}
+
+Resolved resolve_schedule(gbs_weight_type wt, double max_w, uint32_t n, uint64_t m, double delta, double light) {
     Resolved r{};
-    double delta = (p && p->delta > 0) ? p->delta : default_delta(g);
-    double light = (p && p->light >= 0) ? p->light : -1.0;
-    if (g->wtype == GBS_WEIGHT_U32) {
+    if (!(delta > 0)) delta = default_delta(max_w, n, m);
+    if (!(light >= 0)) light = -1.0;
+    if (wt == GBS_WEIGHT_U32) {
         double fd = std::floor(delta);
         r.delta_u = (uint32_t)std::min(std::max(fd, 1.0), 4294967295.0);
         r.delta = r.delta_u;
@@ -260,13 +291,13 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     if (src >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
     gbs_status st = ensure_workspace(g);
     if (st != GBS_OK) return st;
-    const Resolved r = resolve(g, p);
+    const Resolved r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, p ? p->delta : 0.0, p ? p->light : -1.0);
     cudaStream_t s = g->stream;
     const int tb = 256;
     const int eb = std::max(1, std::min<int>((g->n + tb - 1) / tb, g->sms * 8));
     if (!g->mid_valid || g->mid_light_bits != r.light_bits) {
-        k_mid<<<eb, tb, 0, s>>>(g->d_row, g->d_adj, g->n, r.light_bits, g->ws.mid);
-        GBS_CUDA(cudaGetLastError());
+        st = launch_mid(g->d_row, g->d_adj, g->n, r.light_bits, g->ws.mid, g->sms, s);
+        if (st != GBS_OK) return st;
         g->mid_light_bits = r.light_bits;
         g->mid_valid = true;
     }
@@ -293,15 +324,11 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     const bool no_solo = (a.flags & GBS_F_NO_SOLO) != 0;
     a.solo_items = no_solo ? 0u : ((p && p->solo_entries) ? p->solo_entries : 1024u);
     a.solo_desc = no_solo ? 0u : ((p && p->solo_descs) ? p->solo_descs : 64u);
-    uint32_t max_bits;
-    if (g->wtype == GBS_WEIGHT_U32) {
-        max_bits = (uint32_t)g->max_w;
-    } else {
-        const float mf = (float)g->max_w;
-        std::memcpy(&max_bits, &mf, 4);
-    }
-    a.no_heavy = r.light_bits >= max_bits ? 1u : 0u;
+    a.no_heavy = r.light_bits >= max_weight_bits(g->wtype, g->max_w) ? 1u : 0u;
     a.run_ns = a.wait_ns * 16ull;
+    a.group = 0;
+    a.group_ctas = (uint32_t)g->blocks;
+    a.ws.n_cap = g->n;
     if (a.flags & GBS_F_TRACE) {
         if (!g->ws.trace) {
             g->ws.trace_cap = 1u << 20;
@@ -370,7 +397,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     return GBS_OK;
 }
 
-}  // namespace
+}  // namespace gbs
 
 // ===================================================================== C ABI
 extern "C" {
@@ -410,33 +437,11 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
                             const void *weights, gbs_weight_type wtype, gbs_graph **out) {
     if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    if (!row_offsets || (m && (!cols || !weights)))
-        return fail(GBS_ERR_INVALID_ARG, "NULL CSR array");
-    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32)
-        return fail(GBS_ERR_INVALID_ARG, "unknown weight type");
-    if (n == 0 || n > 0x7FFFFFFFu) return fail(GBS_ERR_INVALID_ARG, "vertex count must be in [1, 2^31)");
-    if (m >= 0xFFFFFFFFull) return fail(GBS_ERR_UNSUPPORTED, "edge count must be < 2^32");
-    if (row_offsets[0] != 0 || row_offsets[n] != m)
-        return fail(GBS_ERR_INVALID_ARG, "row_offsets must start at 0 and end at m");
-    for (uint32_t v = 0; v < n; ++v)
-        if (row_offsets[v + 1] < row_offsets[v]) return fail(GBS_ERR_INVALID_ARG, "row_offsets decrease");
-    std::vector<uint32_t> wbits(m);
+    std::vector<uint32_t> row32;
+    std::vector<uint2> adj;
     double max_w = 0.0;
-    for (uint64_t e = 0; e < m; ++e) {
-        if (cols[e] >= n) return fail(GBS_ERR_INVALID_ARG, "column index out of range");
-        if (wtype == GBS_WEIGHT_U32) {
-            const uint32_t w = ((const uint32_t *)weights)[e];
-            wbits[e] = w;
-            if (w > max_w) max_w = w;
-        } else {
-            float w = ((const float *)weights)[e];
-            if (!(w >= 0.0f) || std::isinf(w))
-                return fail(GBS_ERR_INVALID_ARG, "float32 weights must be finite and >= 0");
-            if (w == 0.0f) w = 0.0f;  // -0.0 -> +0.0
-            std::memcpy(&wbits[e], &w, 4);
-            if (w > max_w) max_w = w;
-        }
-    }
+    gbs_status st = prepare_csr(n, m, row_offsets, cols, weights, wtype, row32, adj, max_w);
+    if (st != GBS_OK) return st;
     int dev = 0;
     GBS_CUDA(cudaGetDevice(&dev));
     gbs_graph *g = new gbs_graph();
@@ -457,10 +462,6 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
             return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
         }
     }
-    std::vector<uint2> adj(m);
-    sort_rows(row_offsets, cols, wbits.data(), n, adj);
-    std::vector<uint32_t> row32(n + 1);
-    for (uint32_t v = 0; v <= n; ++v) row32[v] = (uint32_t)row_offsets[v];
     if ((e = cudaMalloc(&g->d_row, sizeof(uint32_t) * (n + 1))) != cudaSuccess ||
         (e = cudaMalloc(&g->d_adj, sizeof(uint2) * (m ? m : 1))) != cudaSuccess ||
         (e = cudaMemcpy(g->d_row, row32.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice)) !=
@@ -488,7 +489,7 @@ gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m, gbs_weig
     if (m) *m = g->m;
     if (wtype) *wtype = g->wtype;
     if (max_weight) *max_weight = g->max_w;
-    if (def_delta) *def_delta = default_delta(g);
+    if (def_delta) *def_delta = default_delta(g->max_w, g->n, g->m);
     return GBS_OK;
 }
 
@@ -576,6 +577,12 @@ gbs_status gbs_device_free(void *p) {
 
 gbs_status gbs_device_synchronize(void) {
     GBS_CUDA(cudaDeviceSynchronize());
+    return GBS_OK;
+}
+
+gbs_status gbs_memcpy(void *dst, const void *src, size_t bytes) {
+    if (bytes && (!dst || !src)) return fail(GBS_ERR_INVALID_ARG, "NULL buffer");
+    if (bytes) GBS_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault));
     return GBS_OK;
 }
 

@@ -1,0 +1,96 @@
+// gbs_host.hpp -- host-side pieces shared by the translation units of
+// libgbsssp: the resident graph handle, error reporting, the bucket schedule
+// resolution and the workspace allocation.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "gbs_sssp_persistent.cuh"
+
+namespace gbs {
+
+// Sets the thread's last-error message and returns the status.
+inline gbs_status fail(gbs_status s, const std::string &msg) {
+    set_last_error(msg.c_str());
+    return s;
+}
+
+#define GBS_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return ::gbs::fail(e_ == cudaErrorMemoryAllocation ? GBS_ERR_NO_MEMORY : GBS_ERR_CUDA, \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+}  // namespace gbs
+
+// A graph resident on one device: CSR with rows sorted by (weight, col), the
+// per-run workspace of the single-source kernel and the cached light split.
+struct gbs_graph {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    gbs_weight_type wtype = GBS_WEIGHT_U32;
+    double max_w = 0.0;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    uint32_t *d_row = nullptr;
+    uint2 *d_adj = nullptr;
+    // workspace
+    bool ws_ready = false;
+    gbs::Workspace ws{};
+    uint32_t *d_dist = nullptr;
+    int32_t *d_pred = nullptr;
+    uint32_t mid_light_bits = 0;
+    bool mid_valid = false;
+    uint32_t epoch = 1, hround = 1;
+    uint32_t trace_n = 0;
+    int blocks = 0;
+    gbs::Ctl host_ctl{};
+};
+
+namespace gbs {
+
+// Bucket width and light bound of one run, as the kernel uses them.
+struct Resolved {
+    double delta, light;
+    uint32_t delta_u, light_bits;
+    float inv_delta_f;
+};
+
+// max weight / average out-degree (1 for an empty graph).
+double default_delta(double max_w, uint32_t n, uint64_t m);
+// delta <= 0 selects default_delta; light < 0 selects light = delta.
+Resolved resolve_schedule(gbs_weight_type wt, double max_w, uint32_t n, uint64_t m, double delta, double light);
+// Bit pattern of the largest weight (uint32 value or float32 bits).
+uint32_t max_weight_bits(gbs_weight_type wt, double max_w);
+
+// Sorts each row by (weight bits, col) into adj (host, all cores).
+void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits, uint32_t n,
+               std::vector<uint2> &adj);
+
+// Validates a host CSR (offsets, targets, weights: finite and >= 0 for
+// float32, -0 stored as +0) and returns its uint32 offsets, its rows sorted
+// by (weight, col) as {col, weight bits} and its largest weight.
+gbs_status prepare_csr(uint32_t n, uint64_t m, const uint64_t *row_offsets, const uint32_t *cols,
+                       const void *weights, gbs_weight_type wtype, std::vector<uint32_t> &row32,
+                       std::vector<uint2> &adj, double &max_w);
+
+// Launches the first-heavy-edge search: mid[v] = first edge of row v whose
+// weight bits exceed light_bits.
+gbs_status launch_mid(const uint32_t *row, const uint2 *adj, uint32_t n, uint32_t light_bits, uint32_t *mid,
+                      int sms, cudaStream_t s);
+
+// Allocates the lists of a workspace for graphs of at most n_cap vertices
+// and m_cap edges (dp, tag, fst, hst, ring, fq, S, pend, desc, ctl; fst, hst
+// and ctl zeroed).  mid and trace are left to the caller.
+gbs_status alloc_workspace(Workspace &w, uint32_t n_cap, uint64_t m_cap, cudaStream_t s);
+void free_workspace(Workspace &w);
+
+// Resident CTAs of the persistent kernels on one SM (0 if they cannot run).
+int persistent_ctas_per_sm(bool f32, bool batch);
+
+}  // namespace gbs

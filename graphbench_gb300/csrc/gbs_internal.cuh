@@ -80,7 +80,8 @@ struct __align__(128) Ctl {
     uint32_t pub_epoch;
     uint32_t pub_hround;
     uint32_t pub_pend_sel;
-    uint32_t pad2[23];
+    uint32_t pub_inst;            // instance being solved (batched launches)
+    uint32_t pad2[22];
     Line ring_cnt[kNB];
     Line fq_cnt[3];
     Line s_cnt[2];
@@ -98,6 +99,7 @@ struct __align__(128) Ctl {
     unsigned long long st_improvements;
     unsigned long long st_reached;
     unsigned long long st_edges_reached;
+    unsigned long long inst_t0;   // globaltimer when the current instance started
 };
 
 struct DevGraph {
@@ -114,12 +116,48 @@ struct Workspace {
     uint32_t *ring, *fq, *S, *pend;
     uint4 *desc;
     uint32_t desc_cap;
+    uint32_t n_cap;         // vertices the per-vertex arrays hold (lists use the
+                            // instance's n as their stride, n <= n_cap)
     TraceRec *trace;
     uint32_t trace_cap;
     Ctl *ctl;
 };
 
-// Everything the persistent kernel needs, passed by value.
+// One instance of a batched launch: a graph, a source and the bucket
+// schedule; dist / pred receive the instance's result (either may be null).
+struct InstDesc {
+    DevGraph g;
+    const uint32_t *mid;    // first heavy edge of each row (row + 1: no split)
+    uint32_t source;
+    uint32_t delta_u;
+    float inv_delta_f;
+    uint32_t no_heavy;
+    uint32_t *dist;
+    int32_t *pred;
+};
+
+// Written by the group that solved the instance (layout = gbs_inst_stats).
+struct InstResult {
+    uint32_t done;          // 1 when the instance completed
+    uint32_t error;         // ErrCode of the group, if it stopped on this instance
+    uint32_t group;
+    uint32_t phases;
+    uint32_t buckets;
+    uint32_t pending_scans;
+    uint32_t solo_phases;
+    uint32_t pad;
+    unsigned long long reached;
+    unsigned long long edges_reached;
+    unsigned long long improvements;
+    unsigned long long start_ns;   // globaltimer at the start and end of the instance
+    unsigned long long end_ns;
+};
+
+constexpr uint32_t kNoInst = 0xFFFFFFFFu;
+
+// Everything the persistent kernel needs, passed by value.  A single-source
+// launch is one group of every CTA; a batched launch cuts the grid into groups
+// of group_ctas CTAs that each own a workspace and take instances from a queue.
 struct SsspArgs {
     DevGraph g;
     Workspace ws;
@@ -132,6 +170,14 @@ struct SsspArgs {
     uint32_t solo_items;    // a SCAN/PENDING phase with at most this many entries runs on one CTA
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
     uint32_t no_heavy;      // the split covers every edge: light scans relax whole rows, no HEAVY phase
+    uint32_t group;         // this CTA's group and the CTAs in one group
+    uint32_t group_ctas;
+    uint32_t *dist_out;     // batched: the current instance's outputs
+    int32_t *pred_out;
+    const InstDesc *inst;   // batched: instances, their results, their count
+    InstResult *res;
+    uint32_t inst_count;
+    uint32_t *queue;        // batched: next instance to take
     unsigned long long wait_ns;   // limit of one barrier wait
     unsigned long long run_ns;    // limit of the whole run
 };

@@ -235,6 +235,9 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.no_heavy = 1;  // every edge is light (see mid above)
     a.wait_ns = 4000ull * 1000000ull;
     a.run_ns = a.wait_ns * 16ull;
+    a.group = 0;
+    a.group_ctas = (uint32_t)(f32 ? d->blocks_f32 : d->blocks_u32);
+    a.ws.n_cap = n;
 
     NA_CUDA(cudaMemsetAsync(a.ws.fst, 0, sizeof(uint32_t) * n, s));
     NA_CUDA(cudaMemsetAsync(a.ws.hst, 0, sizeof(uint32_t) * n, s));

@@ -45,6 +45,10 @@ enum Phase : uint32_t {
     kPhEdges = 3,         // relax the descriptors of the preceding SCAN
     kPhPending = 4,       // re-bucket the pending list
     kPhDone = 5,
+    // batched launches only
+    kPhInit = 6,          // reset the state of a new instance
+    kPhFinish = 7,        // write dist / pred, count reached vertices and edges
+    kPhTake = 8,          // nothing to run: take the first instance
 };
 
 constexpr int kUnroll = 4;
@@ -60,6 +64,7 @@ struct Uniform {
     uint32_t epoch;       // frontier stamp of the current frontier
     uint32_t hround;      // heavy-round stamp (selects the S list)
     uint32_t pend_sel;
+    uint32_t inst;        // batched: instance being solved
     uint32_t gen;         // barrier generation
     unsigned long long t0;  // globaltimer at kernel entry (per CTA)
 };

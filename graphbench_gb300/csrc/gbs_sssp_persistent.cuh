@@ -18,16 +18,21 @@
 
 namespace gbs {
 
-// Who executes a phase: the whole grid or one CTA.
+// Who executes a phase: the CTA group (the whole grid for a single-source
+// launch) or one CTA.
 struct Exec {
     uint32_t tid, nthreads;   // thread index and count over the executors
     uint32_t warp, nwarps;    // warp index and count over the executors
 };
 
-__device__ __forceinline__ Exec grid_exec() {
+__device__ __forceinline__ uint32_t group_rank(const SsspArgs &a) {
+    return blockIdx.x - a.group * a.group_ctas;
+}
+
+__device__ __forceinline__ Exec group_exec(const SsspArgs &a) {
     Exec x;
-    x.tid = blockIdx.x * blockDim.x + threadIdx.x;
-    x.nthreads = gridDim.x * blockDim.x;
+    x.tid = group_rank(a) * blockDim.x + threadIdx.x;
+    x.nthreads = a.group_ctas * blockDim.x;
     x.warp = x.tid >> 5;
     x.nwarps = x.nthreads >> 5;
     return x;
@@ -182,6 +187,58 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     if (lane_id() == 0 && stale) atomicAdd(&ctl->edge_cnt.v, stale);
 }
 
+// ------------------------------------------------------ batched instances
+// INIT: every vertex of the new instance unreached and unqueued, the source
+// at distance 0 (its own predecessor).  The decision that started the
+// instance queued the source in ring bucket 0.  Epoch 1 means the stamps
+// restarted (first use of the workspace, or wrap-around): clear them over the
+// whole workspace, since later instances may be larger.
+__device__ inline void init_instance(const SsspArgs &a, const Uniform &U, const Exec &x) {
+    const uint32_t n = a.g.n;
+    for (uint32_t v = x.tid; v < n; v += x.nthreads) {
+        a.ws.dp[v] = (v == a.source) ? (unsigned long long)a.source : kUnreached;
+        a.ws.tag[v] = (v == a.source) ? 0u : kTagInit;
+    }
+    if (U.epoch == 1u) {
+        for (uint32_t v = x.tid; v < a.ws.n_cap; v += x.nthreads) {
+            a.ws.fst[v] = 0u;
+            a.ws.hst[v] = 0u;
+        }
+    }
+}
+
+// FINISH: packed state -> the caller's dist / pred, and the reached vertices
+// and their out-edges (the GTEPS numerator) summed into the control block.
+template <bool F32>
+__device__ void finish_instance(const SsspArgs &a, const Exec &x, uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t n = a.g.n;
+    Ctl *ctl = a.ws.ctl;
+    unsigned long long r = 0, e = 0;
+    for (uint32_t v = x.tid; v < n; v += x.nthreads) {
+        const unsigned long long p = __ldcg(a.ws.dp + v);
+        const bool reached = p != kUnreached;
+        if (a.dist_out) a.dist_out[v] = reached ? (uint32_t)(p >> 32) : (F32 ? 0x7F800000u : 0xFFFFFFFFu);
+        if (a.pred_out) a.pred_out[v] = reached ? (v == a.source ? (int32_t)v : (int32_t)(uint32_t)p) : -1;
+        if (reached) {
+            ++r;
+            e += __ldg(a.g.row + v + 1) - __ldg(a.g.row + v);
+        }
+    }
+    unsigned long long im = imp;
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        e += __shfl_down_sync(FULL, e, o);
+        im += __shfl_down_sync(FULL, im, o);
+    }
+    if (lane_id() == 0) {
+        if (r) atomicAdd(&ctl->st_reached, r);
+        if (e) atomicAdd(&ctl->st_edges_reached, e);
+        if (im) atomicAdd(&ctl->st_improvements, im);
+    }
+    imp = 0;
+}
+
 // Runs the phase U.phase with executor x (grid or one CTA).
 template <bool F32>
 __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
@@ -217,6 +274,12 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
         case kPhPending:
             rebucket_pending<F32>(a, U, x, scr);
             break;
+        case kPhInit:
+            init_instance(a, U, x);
+            break;
+        case kPhFinish:
+            finish_instance<F32>(a, x, imp);
+            break;
         default:
             break;
     }
@@ -248,7 +311,10 @@ __device__ __forceinline__ Uniform advance_uniform(const Uniform &U, uint32_t ne
 // finished it (or is waiting while this CTA runs alone), so all counters are
 // at rest.  Decides the next phase, resets the lists it appends to, records
 // statistics and the trace, publishes the new state and says whether the next
-// phase is small enough for this CTA to run alone.
+// phase is small enough for this CTA to run alone.  In a batched launch the
+// end of a run leads to FINISH, and after FINISH the group takes the next
+// instance from the queue (INIT) or stops.
+template <bool Batch>
 __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool was_solo, bool &solo) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
@@ -277,7 +343,15 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     bool need_ring_scan = false;
     bool bucket_end = false;
     uint32_t scan_from = 0;
-    if (U.phase == kPhPending) {
+    bool take = false;
+    if (Batch && U.phase >= kPhInit) {
+        if (U.phase == kPhInit) {
+            next = kPhLightFirst;   // bucket 0 holds the source
+            nb = 0;
+        } else {
+            take = true;            // after FINISH, or at the start of the launch
+        }
+    } else if (U.phase == kPhPending) {
         ps2 ^= 1u;
         need_ring_scan = true;
         scan_from = U.W;
@@ -316,8 +390,15 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             next = kPhLightFirst;
             nb = found;
         } else {
-            next = kPhDone;
+            next = Batch ? kPhFinish : kPhDone;
         }
+    }
+    uint32_t inst = U.inst;
+    if (take) {
+        if (lane == 0) inst = atomicAdd(a.queue, 1u);
+        inst = __shfl_sync(FULL, inst, 0);
+        next = inst < a.inst_count ? kPhInit : kPhDone;
+        if (next == kPhDone) inst = kNoInst;
     }
     // whole-run limit: a run that has not finished within run_ns is stopped
     if (globaltimer() - U.t0 > a.run_ns) {
@@ -325,7 +406,17 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
     }
     if (err) next = kPhDone;
-    const Uniform N = advance_uniform(U, next, nb);
+    Uniform N = advance_uniform(U, next, nb);
+    if (take) {
+        N.inst = inst;
+        N.hround += 1u;   // the last heavy round of the previous instance may be stamped
+        // stamps restart at 1 on a fresh workspace or before they wrap; INIT
+        // then clears them
+        if (U.epoch == 0u || U.epoch > 0xF0000000u || U.hround > 0xF0000000u) {
+            N.epoch = 1u;
+            N.hround = 1u;
+        }
+    }
     // size of the next phase's input
     uint32_t items = 0;
     switch (next) {
@@ -337,8 +428,9 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         default: break;
     }
     // re-bucketing always runs on the grid: run on one CTA it lost survivors
-    // (measured; cause not yet understood), and it happens a few times per run
-    solo = next != kPhDone && next != kPhPending &&
+    // (measured; cause not yet understood), and it happens a few times per run.
+    // INIT and FINISH (batched launches) always run on the whole group.
+    solo = next < kPhDone && next != kPhPending &&
            (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
     if (lane == 0) {
         if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
@@ -364,7 +456,24 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             }
             ctl->trace_n = ti + 1;
         }
-        ctl->st_phases += 1;
+        if (Batch && U.inst != kNoInst && (U.phase == kPhFinish || err)) {
+            InstResult r;
+            r.done = (U.phase == kPhFinish && !err) ? 1u : 0u;
+            r.error = err;
+            r.group = a.group;
+            r.phases = ctl->st_phases;
+            r.buckets = ctl->st_buckets;
+            r.pending_scans = ctl->st_pending_scans;
+            r.solo_phases = ctl->st_solo_phases;
+            r.pad = 0;
+            r.reached = __ldcg(&ctl->st_reached);
+            r.edges_reached = __ldcg(&ctl->st_edges_reached);
+            r.improvements = __ldcg(&ctl->st_improvements);
+            r.start_ns = ctl->inst_t0;
+            r.end_ns = globaltimer();
+            a.res[U.inst] = r;
+        }
+        if (U.phase < kPhDone) ctl->st_phases += 1;
         if (U.phase == kPhLightFirst) ctl->st_buckets += 1;
         if (U.phase == kPhPending) {
             ctl->st_pending_scans += 1;
@@ -387,6 +496,34 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         ctl->pub_epoch = N.epoch;
         ctl->pub_hround = N.hround;
         ctl->pub_pend_sel = N.pend_sel;
+        ctl->pub_inst = N.inst;
+    }
+    if (take && next == kPhInit) {
+        // every list of the new instance starts empty; the source waits in
+        // ring bucket 0 (list slot 0, entry 0)
+        ctl->ring_cnt[lane].v = 0u;
+        ctl->ring_cnt[lane + 32].v = 0u;
+        __syncwarp();
+        if (lane == 0) {
+            ctl->ring_cnt[0].v = 1u;
+            a.ws.ring[0] = a.inst[inst].source;
+            for (int i = 0; i < 3; ++i) ctl->fq_cnt[i].v = 0u;
+            for (int i = 0; i < 2; ++i) {
+                ctl->s_cnt[i].v = 0u;
+                ctl->pend_cnt[i].v = 0u;
+                ctl->pend_min[i].v = kTagInit;
+            }
+            ctl->desc_cnt.v = 0u;
+            ctl->edge_cnt.v = 0u;
+            ctl->st_buckets = 0u;
+            ctl->st_phases = 0u;
+            ctl->st_pending_scans = 0u;
+            ctl->st_solo_phases = 0u;
+            ctl->st_improvements = 0ull;
+            ctl->st_reached = 0ull;
+            ctl->st_edges_reached = 0ull;
+            ctl->inst_t0 = globaltimer();
+        }
     }
     __syncwarp();
 }
@@ -401,6 +538,7 @@ __device__ __forceinline__ void fetch_published(Ctl *ctl, uint32_t *s_pub) {
     s_pub[4] = ld_relaxed(&ctl->pub_epoch);
     s_pub[5] = ld_relaxed(&ctl->pub_hround);
     s_pub[6] = ld_relaxed(&ctl->pub_pend_sel);
+    s_pub[7] = ld_relaxed(&ctl->pub_inst);
 }
 
 __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &U) {
@@ -411,6 +549,7 @@ __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &
     U.epoch = s_pub[4];
     U.hround = s_pub[5];
     U.pend_sel = s_pub[6];
+    U.inst = s_pub[7];
 }
 
 // Grid barrier after a phase.  The CTA that arrives last decides the next
@@ -419,7 +558,7 @@ __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &
 // published state.  Every wait is bounded by a.wait_ns (globaltimer); on
 // expiry the error word is set and every CTA leaves at its next check.  A
 // solo stretch stops after a.wait_ns / 4 so the waiting CTAs never time out.
-template <bool F32>
+template <bool F32, bool Batch>
 __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U, WarpScratch *scr,
                                                    uint32_t &imp) {
     Ctl *ctl = a.ws.ctl;
@@ -428,11 +567,11 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
     __syncthreads();
     if (threadIdx.x == 0) {
         // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
-        const bool stall = (a.flags & GBS_F_TEST_STALL) && U.gen == 0 && blockIdx.x == 0;
+        const bool stall = (a.flags & GBS_F_TEST_STALL) && U.gen == 0 && group_rank(a) == 0;
         uint32_t last = 0;
         if (!stall) {
             __threadfence();
-            last = atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1u;
+            last = atomicAdd(&ctl->bar_count, 1u) == a.group_ctas - 1u;
             if (last) __threadfence();
         }
         s_flag[0] = last;
@@ -444,7 +583,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
         for (;;) {
             if (threadIdx.x < 32) {
                 bool solo = false;
-                control_step(a, U, was_solo, solo);
+                control_step<Batch>(a, U, was_solo, solo);
                 if (threadIdx.x == 0) {
                     s_flag[1] = solo && (globaltimer() - ts) < a.wait_ns / 4;
                     fetch_published(ctl, s_pub);
@@ -505,18 +644,78 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     U.epoch = a.epoch0;
     U.hround = a.hround0;
     U.pend_sel = 0;
+    U.inst = kNoInst;
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t imp = 0;
     while (U.phase != kPhDone) {
-        run_phase<F32>(a, U, grid_exec(), scr, imp);
-        barrier_and_decide<F32>(a, U, scr, imp);
+        run_phase<F32>(a, U, group_exec(a), scr, imp);
+        barrier_and_decide<F32, false>(a, U, scr, imp);
     }
     for (int o = 16; o > 0; o >>= 1) imp += __shfl_down_sync(0xffffffffu, imp, o);
     if (lane_id() == 0 && imp) atomicAdd(&ctl->st_improvements, (unsigned long long)imp);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctl->next_epoch = U.epoch;        // next free stamps for the following run
         ctl->next_hround = U.hround;
+    }
+}
+
+// Batched launch: CTA group g (group_ctas CTAs) owns workspace ws_groups[g]
+// and solves instances taken from base.queue until the queue is empty.  The
+// control block of a workspace keeps the last stamps between launches.
+template <bool F32>
+__global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Workspace *__restrict__ ws_groups) {
+    __shared__ SsspArgs s_a;
+    __shared__ WarpScratch s_scr[kTPB / 32];
+    WarpScratch *scr = &s_scr[threadIdx.x >> 5];
+    const uint32_t group = blockIdx.x / base.group_ctas;
+    if (threadIdx.x == 0) {
+        s_a = base;
+        s_a.group = group;
+        s_a.ws = ws_groups[group];
+    }
+    __syncthreads();
+    Ctl *ctl = s_a.ws.ctl;
+    Uniform U;
+    U.phase = kPhTake;
+    U.logical = kPhLight;
+    U.b = 0;
+    U.W = 0;
+    U.epoch = ld_relaxed(&ctl->next_epoch);
+    U.hround = ld_relaxed(&ctl->next_hround);
+    U.pend_sel = 0;
+    U.inst = kNoInst;
+    U.gen = 0;
+    U.t0 = globaltimer();
+    uint32_t loaded = kNoInst;
+    uint32_t imp = 0;
+    while (U.phase != kPhDone) {
+        if (U.inst != loaded) {
+            // a new instance: its graph, source, schedule and outputs
+            if (threadIdx.x == 0) {
+                const InstDesc d = s_a.inst[U.inst];
+                s_a.g = d.g;
+                s_a.ws.mid = const_cast<uint32_t *>(d.mid);
+                s_a.source = d.source;
+                s_a.delta_u = d.delta_u;
+                s_a.inv_delta_f = d.inv_delta_f;
+                s_a.no_heavy = d.no_heavy;
+                s_a.dist_out = d.dist;
+                s_a.pred_out = d.pred;
+            }
+            __syncthreads();
+            loaded = U.inst;
+            U.t0 = globaltimer();   // the run-time limit applies per instance
+        }
+        run_phase<F32>(s_a, U, group_exec(s_a), scr, imp);
+        barrier_and_decide<F32, true>(s_a, U, scr, imp);
+    }
+    if (group_rank(s_a) == 0 && threadIdx.x == 0) {
+        // after an error the stamps in flight are unknown: 0 makes the next
+        // launch clear them
+        const bool err = ld_relaxed(&ctl->error) != 0;
+        ctl->next_epoch = err ? 0u : U.epoch;
+        ctl->next_hround = err ? 0u : U.hround;
     }
 }
 

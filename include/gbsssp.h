@@ -178,6 +178,105 @@ typedef struct gbs_phase_rec {
 gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *count);
 
 /*
+ * Batched SSSP: many independent instances in one persistent launch.
+ *
+ * The reference solves several sources one after the other, as the source
+ * loop of its betweenness centrality (btwcentral/csr_bc.c:16-123 calls
+ * run_sspath per source); it has no batched call.  Here a plan fixes a set of
+ * instances -- K sources on one resident graph (gbs_plan_sources) or one
+ * source on each graph of a pack of independent graphs (gbs_plan_pack) --
+ * with their bucket schedules and device outputs.  The launch cuts the grid
+ * into groups of group_ctas CTAs; each group owns its own bucket queues and
+ * takes instances from a shared queue until none is left.  The launch
+ * sequence is captured in a CUDA graph once and replayed by gbs_plan_launch.
+ * Results equal gbs_sssp's bit for bit, instance by instance.
+ */
+typedef struct gbs_pack gbs_pack;
+typedef struct gbs_plan gbs_plan;
+
+/* One host CSR of a pack (same layout as gbs_graph_create's arguments). */
+typedef struct gbs_csr_view {
+    uint32_t n;
+    uint64_t m;
+    const uint64_t *row_offsets;   /* n+1, exclusive */
+    const uint32_t *cols;          /* m */
+    const void *weights;           /* m uint32 or float32 */
+} gbs_csr_view;
+
+typedef struct gbs_batch_params {
+    double delta;          /* > 0: bucket width of every instance; <= 0: the
+                              graph's default (max weight / average out-degree)
+                              times delta_scale */
+    double delta_scale;    /* multiplier of the default width (<= 0: 1) */
+    double light;          /* >= 0: light bound of every instance; < 0: the
+                              instance's delta; +INFINITY: no split (every edge
+                              light) */
+    uint32_t group_ctas;   /* CTAs per group (0: chosen from the instance count) */
+    uint32_t flags;        /* GBS_F_NO_SOLO */
+    uint32_t wait_limit_ms;
+    uint32_t solo_entries;
+    uint32_t solo_descs;
+    uint32_t reserved;
+} gbs_batch_params;
+
+/* Per-instance result record (device times from %globaltimer). */
+typedef struct gbs_inst_stats {
+    uint32_t done;           /* 1 when the instance completed */
+    uint32_t error;          /* device error code of its group (0 = none) */
+    uint32_t group;
+    uint32_t phases;
+    uint32_t buckets;
+    uint32_t pending_scans;
+    uint32_t solo_phases;
+    uint32_t pad;
+    uint64_t reached;
+    uint64_t edges_reached;
+    uint64_t improvements;
+    uint64_t start_ns;
+    uint64_t end_ns;
+} gbs_inst_stats;
+
+typedef struct gbs_batch_stats {
+    double device_ms;        /* the whole graph launch (CUDA events) */
+    uint32_t instances;
+    uint32_t completed;
+    uint32_t groups;
+    uint32_t group_ctas;
+    uint32_t blocks;
+    uint32_t max_phases;
+    uint64_t phases;
+    uint64_t reached;
+    uint64_t edges_reached;  /* GTEPS numerator summed over instances */
+} gbs_batch_stats;
+
+/* Uploads count host CSRs into one device allocation (rows sorted as in
+ * gbs_graph_create).  Same validation; every graph has the same wtype. */
+gbs_status gbs_pack_create(uint32_t count, const gbs_csr_view *graphs, gbs_weight_type wtype,
+                           gbs_pack **out);
+gbs_status gbs_pack_destroy(gbs_pack *p);
+/* vertex_offsets (count+1, may be NULL) receives where each graph's vertices
+ * start in a pack-wide vertex array: the layout of gbs_plan_pack's outputs. */
+gbs_status gbs_pack_info(const gbs_pack *p, uint32_t *count, uint64_t *total_n, uint64_t *total_m,
+                         uint64_t *vertex_offsets);
+
+/* K sources on g.  dist_dev: k*n uint32/float32 (instance i at i*n), pred_dev:
+ * k*n int32 or NULL.  g must outlive the plan. */
+gbs_status gbs_plan_sources(gbs_graph *g, const uint32_t *sources, uint32_t k,
+                            const gbs_batch_params *params, void *dist_dev, int32_t *pred_dev,
+                            gbs_plan **out);
+/* sources[i] on graph i of the pack.  dist_dev / pred_dev: total_n entries
+ * in the gbs_pack_info vertex layout.  The pack must outlive the plan. */
+gbs_status gbs_plan_pack(gbs_pack *p, const uint32_t *sources, const gbs_batch_params *params,
+                         void *dist_dev, int32_t *pred_dev, gbs_plan **out);
+/* Replays the captured launch on the plan's stream and returns at once. */
+gbs_status gbs_plan_launch(gbs_plan *plan);
+/* Waits for the last launch; per_instance (instances entries) may be NULL.
+ * Returns the first device error, or GBS_ERR_TIMEOUT if instances were left
+ * unsolved. */
+gbs_status gbs_plan_wait(gbs_plan *plan, gbs_batch_stats *stats, gbs_inst_stats *per_instance);
+gbs_status gbs_plan_destroy(gbs_plan *plan);
+
+/*
  * SSSP that allocates no memory (no counterpart in the reference).  For
  * callers that cannot call cudaMalloc/cudaFree while serving a query: a host
  * application that owns all device memory through its own pool, or a
@@ -211,6 +310,8 @@ gbs_status gbs_device_alloc(size_t bytes, void **out);
 gbs_status gbs_device_free(void *p);
 /* Blocks until all work the library queued on the device has finished. */
 gbs_status gbs_device_synchronize(void);
+/* Synchronous copy between any host and device buffers (cudaMemcpyDefault). */
+gbs_status gbs_memcpy(void *dst, const void *src, size_t bytes);
 
 /*
  * Synthetic inputs (host-side C generators; deterministic for a given seed).
