@@ -19,6 +19,9 @@ ROOT = PKG.parent
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libgbsssp.so"
+# run_sspath_arr / run_sspath over the reference's t_csr (include/gbsssp_compat.h)
+COMPAT_LIB = PKG / "libgbsssp_compat.so"
+COMPAT_SOURCES = ["host/compat.c"]
 
 CUDA_SOURCES = ["csrc/gbs_api.cu", "csrc/gbs_batch.cu", "csrc/gbs_noalloc.cu"]
 C_SOURCES = ["host/gen.c"]
@@ -40,9 +43,9 @@ def _deps() -> list[Path]:
 
 
 def _stale() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or not COMPAT_LIB.exists():
         return True
-    t = LIB.stat().st_mtime
+    t = min(LIB.stat().st_mtime, COMPAT_LIB.stat().st_mtime)
     return any(p.stat().st_mtime > t for p in _deps() if p.is_file())
 
 
@@ -75,6 +78,11 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     tmp = LIB.with_suffix(".so.tmp")
     _run([nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-pthread"])
     os.replace(tmp, LIB)
+    ctmp = COMPAT_LIB.with_suffix(".so.tmp")
+    _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-D_GNU_SOURCE", "-pthread", "-I", str(INCLUDE),
+          *[str(PKG / c) for c in COMPAT_SOURCES], "-o", str(ctmp), "-L", str(PKG), "-lgbsssp",
+          "-Wl,-rpath,$ORIGIN", "-lm"])
+    os.replace(ctmp, COMPAT_LIB)
     return LIB
 
 
