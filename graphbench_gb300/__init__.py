@@ -22,6 +22,7 @@ import numpy as np
 
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "libgbsssp.so"
+COMPAT_LIB_PATH = _PKG / "libgbsssp_compat.so"   # run_sspath_arr / run_sspath over t_csr
 
 STATUS = {
     0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "NO_MEMORY", 4: "CAPACITY",
@@ -37,6 +38,7 @@ EXPORTS = [
     "gbs_sssp_multi", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
     "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
     "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
+    "gbs_autotune", "gbs_autotune_plan_sources", "gbs_autotune_plan_pack",
     "gbs_device_alloc", "gbs_device_free",
     "gbs_device_synchronize", "gbs_memcpy",
     "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
@@ -53,7 +55,8 @@ class GbsError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
                 ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
-                ("solo_entries", ctypes.c_uint32), ("solo_descs", ctypes.c_uint32)]
+                ("solo_entries", ctypes.c_uint32), ("solo_descs", ctypes.c_uint32),
+                ("inline_edges", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class PhaseRec(ctypes.Structure):
@@ -90,7 +93,7 @@ class BatchParams(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("delta_scale", ctypes.c_double), ("light", ctypes.c_double),
                 ("group_ctas", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("wait_limit_ms", ctypes.c_uint32), ("solo_entries", ctypes.c_uint32),
-                ("solo_descs", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("solo_descs", ctypes.c_uint32), ("inline_edges", ctypes.c_uint32)]
 
 
 class InstStats(ctypes.Structure):
@@ -109,6 +112,21 @@ class BatchStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("best", Params), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("delta_scale", ctypes.c_double), ("candidates", ctypes.c_uint32), ("runs", ctypes.c_uint32),
+                ("no_split", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
+
+
+class BatchTuneReport(ctypes.Structure):
+    _fields_ = [("best", BatchParams), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("candidates", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+def _struct_dict(s) -> dict:
+    return {k: getattr(s, k) for k, _ in s._fields_}
 
 
 class HostCsr(ctypes.Structure):
@@ -158,6 +176,10 @@ def _load() -> ctypes.CDLL:
     L.gbs_plan_launch.argtypes = [P]
     L.gbs_plan_wait.argtypes = [P, ctypes.POINTER(BatchStats), P]
     L.gbs_plan_destroy.argtypes = [P]
+    L.gbs_autotune.argtypes = [P, P, ctypes.c_uint32, ctypes.c_double, ctypes.POINTER(TuneReport)]
+    L.gbs_autotune_plan_sources.argtypes = [P, P, ctypes.c_uint32, ctypes.c_double,
+                                            ctypes.POINTER(BatchTuneReport)]
+    L.gbs_autotune_plan_pack.argtypes = [P, P, ctypes.c_double, ctypes.POINTER(BatchTuneReport)]
     return L
 
 
@@ -347,7 +369,8 @@ class Graph:
 
     @staticmethod
     def params(delta: float | None = None, light: float | None = None, flags: int = 0,
-               wait_limit_ms: int = 0, solo_entries: int = 0, solo_descs: int = 0) -> Params:
+               wait_limit_ms: int = 0, solo_entries: int = 0, solo_descs: int = 0,
+               inline_edges: int = 0) -> Params:
         p = Params()
         p.delta = float(delta) if delta else 0.0
         p.light = float(light) if light is not None else -1.0
@@ -355,6 +378,7 @@ class Graph:
         p.wait_limit_ms = wait_limit_ms
         p.solo_entries = solo_entries
         p.solo_descs = solo_descs
+        p.inline_edges = inline_edges
         return p
 
     def trace(self) -> list[dict]:
@@ -391,6 +415,19 @@ class Graph:
         _check(lib.gbs_sssp_device(self._h, int(source), ctypes.byref(p), dist_ptr, pred_ptr,
                                    ctypes.byref(st)), "gbs_sssp_device")
         return st.as_dict()
+
+    def autotune(self, sources, budget_ms: float = 0.0):
+        """Fastest schedule on these sources (gbs_autotune).  Returns (kwargs
+        for sssp / sssp_device, report dict)."""
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        rep = TuneReport()
+        _check(lib.gbs_autotune(self._h, _ptr(src), len(src), float(budget_ms), ctypes.byref(rep)), "gbs_autotune")
+        b = rep.best
+        kw = {"delta": b.delta, "light": b.light, "solo_entries": b.solo_entries, "solo_descs": b.solo_descs,
+              "inline_edges": b.inline_edges}
+        r = {k: getattr(rep, k) for k, _ in TuneReport._fields_ if k != "best"}
+        r["best"] = dict(kw)
+        return kw, r
 
     def sssp_multi(self, sources, delta: float | None = None, light: float | None = None,
                    want_dist: bool = True, want_pred: bool = False, **kw):
@@ -456,7 +493,7 @@ def run_sspath_arr(gs: TCsr, source: int, delta: float) -> np.ndarray:
 # --------------------------------------------------------------- batched
 def batch_params(delta: float | None = None, delta_scale: float | None = None, light: float | None = None,
                  group_ctas: int = 0, flags: int = 0, wait_limit_ms: int = 0, solo_entries: int = 0,
-                 solo_descs: int = 0) -> BatchParams:
+                 solo_descs: int = 0, inline_edges: int = 0) -> BatchParams:
     """light=None: light bound = delta; light=math.inf: no light/heavy split."""
     p = BatchParams()
     p.delta = float(delta) if delta else 0.0
@@ -467,6 +504,7 @@ def batch_params(delta: float | None = None, delta_scale: float | None = None, l
     p.wait_limit_ms = wait_limit_ms
     p.solo_entries = solo_entries
     p.solo_descs = solo_descs
+    p.inline_edges = inline_edges
     return p
 
 
@@ -598,3 +636,21 @@ class Plan:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def autotune_plan(target, sources, budget_ms: float = 0.0):
+    """Fastest batched parameters (CTAs per group, schedule) for a Plan over
+    target (Graph or Pack) and sources.  Returns (BatchParams, report dict)."""
+    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    rep = BatchTuneReport()
+    if isinstance(target, Graph):
+        _check(lib.gbs_autotune_plan_sources(target.handle, _ptr(src), len(src), float(budget_ms),
+                                             ctypes.byref(rep)), "gbs_autotune_plan_sources")
+    else:
+        _check(lib.gbs_autotune_plan_pack(target._h, _ptr(src), float(budget_ms), ctypes.byref(rep)),
+               "gbs_autotune_plan_pack")
+    best = BatchParams()
+    ctypes.memmove(ctypes.byref(best), ctypes.byref(rep.best), ctypes.sizeof(BatchParams))
+    r = {"best_ms": rep.best_ms, "default_ms": rep.default_ms, "candidates": rep.candidates,
+         "best": _struct_dict(best)}
+    return best, r

@@ -325,6 +325,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.solo_items = no_solo ? 0u : ((p && p->solo_entries) ? p->solo_entries : 1024u);
     a.solo_desc = no_solo ? 0u : ((p && p->solo_descs) ? p->solo_descs : 64u);
     a.no_heavy = r.light_bits >= max_weight_bits(g->wtype, g->max_w) ? 1u : 0u;
+    a.inline_max = (p && p->inline_edges) ? p->inline_edges : kInlineEdges;
     a.run_ns = a.wait_ns * 16ull;
     a.group = 0;
     a.group_ctas = (uint32_t)g->blocks;

@@ -170,6 +170,7 @@ struct SsspArgs {
     uint32_t solo_items;    // a SCAN/PENDING phase with at most this many entries runs on one CTA
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
     uint32_t no_heavy;      // the split covers every edge: light scans relax whole rows, no HEAVY phase
+    uint32_t inline_max;    // rows up to this long are relaxed by the scanning warp
     uint32_t group;         // this CTA's group and the CTAs in one group
     uint32_t group_ctas;
     uint32_t *dist_out;     // batched: the current instance's outputs

@@ -233,6 +233,7 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.solo_items = 1024;
     a.solo_desc = 64;
     a.no_heavy = 1;  // every edge is light (see mid above)
+    a.inline_max = kInlineEdges;
     a.wait_ns = 4000ull * 1000000ull;
     a.run_ns = a.wait_ns * 16ull;
     a.group = 0;

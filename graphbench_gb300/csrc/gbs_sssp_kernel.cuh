@@ -23,7 +23,7 @@
 //
 // Each LIGHT/HEAVY step is one or two grid phases:
 //   SCAN   one thread per frontier entry: validate and read the row range.
-//          Rows of at most kInlineEdges edges are relaxed right away by the
+//          Rows of at most inline_max edges are relaxed right away by the
 //          scanning warp; longer rows become edge descriptors {u, dist(u),
 //          first, end} of at most kDescEdges edges (the reference's request
 //          list R, without one triple per edge).
@@ -53,7 +53,7 @@ enum Phase : uint32_t {
 
 constexpr int kUnroll = 4;
 constexpr uint32_t kDescEdges = 32u * kUnroll;   // edges per descriptor (one warp round)
-constexpr uint32_t kInlineEdges = 32u;           // rows up to this long are relaxed in SCAN
+constexpr uint32_t kInlineEdges = 32u;           // default inline_max: rows up to this long are relaxed in SCAN
 
 // Values identical in every CTA (the kernel's uniform state).
 struct Uniform {

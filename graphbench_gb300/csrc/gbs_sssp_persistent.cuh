@@ -81,7 +81,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
         if (ok && add_s) hold = atomicExch(a.ws.hst + u, hround);
         const uint32_t len = e - s;
         // long rows -> descriptors, reserved with one atomic per warp
-        const uint32_t nd = len > kInlineEdges ? (len + kDescEdges - 1) / kDescEdges : 0u;
+        const uint32_t nd = len > a.inline_max ? (len + kDescEdges - 1) / kDescEdges : 0u;
         uint32_t incl = nd;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {

@@ -1,0 +1,245 @@
+// gbs_tune.cu -- the schedule autotuner (gbs_autotune, gbs_autotune_plan_*).
+//
+// Host-only: candidates run through the public entry points and are timed by
+// the kernel's CUDA events (single source: kernel_ms, the persistent launch
+// alone; batched: the graph launch).  The result of any schedule is the same
+// least fixpoint, so the search only compares times.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbs_host.hpp"
+
+using namespace gbs;
+
+namespace {
+
+// Default width multipliers and knob values explored around the best.
+const double kScales[] = {0.25, 0.5, 1.0, 2.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0, 256.0, 512.0, 1024.0, 4096.0};
+const uint32_t kInline[] = {8, 16, 64, 128};
+const uint32_t kSoloEntries[] = {256, 4096, 16384};
+const uint32_t kSoloDescs[] = {16, 256, 1024};
+
+struct Budget {
+    double limit_ms, used_ms = 0.0;
+    bool left() const { return used_ms < limit_ms; }
+};
+
+// Mean kernel time per source of one schedule (one untimed warm-up run).
+gbs_status time_single(gbs_graph *g, const std::vector<uint32_t> &src, const gbs_params &p, Budget &b,
+                       uint32_t &runs, double &mean_ms) {
+    gbs_stats st;
+    gbs_params q = p;
+    q.flags |= GBS_F_NO_STATS;
+    gbs_status s = gbs_sssp_device(g, src[0], &q, nullptr, nullptr, &st);
+    if (s != GBS_OK) return s;
+    ++runs;
+    b.used_ms += st.kernel_ms;
+    double sum = 0.0;
+    for (uint32_t x : src) {
+        s = gbs_sssp_device(g, x, &q, nullptr, nullptr, &st);
+        if (s != GBS_OK) return s;
+        ++runs;
+        sum += st.kernel_ms;
+        b.used_ms += st.kernel_ms;
+    }
+    mean_ms = sum / (double)src.size();
+    return GBS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, double budget_ms,
+                        gbs_tune_report *out) {
+    if (!g || !sources || count == 0 || !out) return fail(GBS_ERR_INVALID_ARG, "graph, sources and out are required");
+    std::vector<uint32_t> src(sources, sources + count);
+    for (uint32_t x : src)
+        if (x >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
+    Budget b{budget_ms > 0 ? budget_ms : 4000.0};
+    std::memset(out, 0, sizeof(*out));
+    const double d0 = default_delta(g->max_w, g->n, g->m);
+    gbs_params base{};
+    base.light = -1.0;
+    double best_ms = 0.0;
+    gbs_status s = time_single(g, src, base, b, out->runs, best_ms);
+    if (s != GBS_OK) return s;
+    out->default_ms = best_ms;
+    out->candidates = 1;
+    gbs_params best = base;
+    best.delta = d0;
+    double best_scale = 1.0;
+    bool best_nosplit = false;
+    // 1. width for each split: walk the scales, stop two steps past a minimum
+    for (int split = 0; split < 2 && b.left(); ++split) {
+        double local_best = INFINITY;
+        int worse = 0;
+        for (double sc : kScales) {
+            if (!b.left() || worse >= 2) break;
+            if (split == 0 && sc == 1.0) {   // the default, timed above
+                local_best = out->default_ms;
+                continue;
+            }
+            gbs_params p = base;
+            p.delta = d0 * sc;
+            p.light = split ? INFINITY : -1.0;
+            double ms = 0.0;
+            if ((s = time_single(g, src, p, b, out->runs, ms)) != GBS_OK) return s;
+            ++out->candidates;
+            if (ms < local_best) {
+                local_best = ms;
+                worse = 0;
+            } else {
+                ++worse;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = p;
+                best_scale = sc;
+                best_nosplit = split != 0;
+            }
+        }
+    }
+    // 2. the other knobs, one at a time around the best
+    auto try_knob = [&](auto set) -> gbs_status {
+        if (!b.left()) return GBS_OK;
+        gbs_params p = best;
+        set(p);
+        double ms = 0.0;
+        gbs_status r = time_single(g, src, p, b, out->runs, ms);
+        if (r != GBS_OK) return r;
+        ++out->candidates;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = p;
+        }
+        return GBS_OK;
+    };
+    for (uint32_t v : kInline)
+        if ((s = try_knob([&](gbs_params &p) { p.inline_edges = v; })) != GBS_OK) return s;
+    for (uint32_t v : kSoloEntries)
+        if ((s = try_knob([&](gbs_params &p) { p.solo_entries = v; })) != GBS_OK) return s;
+    for (uint32_t v : kSoloDescs)
+        if ((s = try_knob([&](gbs_params &p) { p.solo_descs = v; })) != GBS_OK) return s;
+    // explicit values in the returned schedule
+    if (!(best.delta > 0)) best.delta = d0;
+    best.flags = 0;
+    out->best = best;
+    out->best_ms = best_ms;
+    out->delta_scale = best_scale;
+    out->no_split = best_nosplit ? 1 : 0;
+    return GBS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Creates a plan without outputs, runs it once untimed and once timed.
+template <class Make>
+gbs_status time_plan(Make make, const gbs_batch_params &bp, Budget &b, double &ms) {
+    gbs_plan *plan = nullptr;
+    gbs_status s = make(bp, &plan);
+    if (s != GBS_OK) return s;
+    gbs_batch_stats st;
+    for (int rep = 0; rep < 2 && s == GBS_OK; ++rep) {
+        s = gbs_plan_launch(plan);
+        if (s == GBS_OK) s = gbs_plan_wait(plan, &st, nullptr);
+        if (s == GBS_OK) b.used_ms += st.device_ms;
+    }
+    gbs_plan_destroy(plan);
+    ms = st.device_ms;
+    return s;
+}
+
+template <class Make>
+gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, gbs_batch_tune_report *out) {
+    Budget b{budget_ms > 0 ? budget_ms : 4000.0};
+    std::memset(out, 0, sizeof(*out));
+    gbs_batch_params base{};
+    base.light = -1.0;
+    double ms = 0.0;
+    gbs_status s = time_plan(make, base, b, ms);
+    if (s != GBS_OK) return s;
+    out->default_ms = ms;
+    out->candidates = 1;
+    gbs_batch_params best = base;
+    double best_ms = ms;
+    auto consider = [&](const gbs_batch_params &p) -> gbs_status {
+        if (!b.left()) return GBS_OK;
+        double t = 0.0;
+        gbs_status r = time_plan(make, p, b, t);
+        if (r == GBS_ERR_NO_MEMORY) return GBS_OK;   // a shape that does not fit is skipped
+        if (r != GBS_OK) return r;
+        ++out->candidates;
+        if (t < best_ms) {
+            best_ms = t;
+            best = p;
+        }
+        return GBS_OK;
+    };
+    // 1. CTAs per group (powers of two and the divisors of the SM count)
+    std::vector<uint32_t> shapes;
+    for (uint32_t gc = 1; gc <= max_blocks; gc *= 2) shapes.push_back(gc);
+    for (uint32_t d = 3; d <= max_blocks; ++d)
+        if (max_blocks % d == 0 && (d & (d - 1)) != 0) shapes.push_back(d);
+    std::sort(shapes.begin(), shapes.end());
+    for (uint32_t gc : shapes) {
+        gbs_batch_params p = base;
+        p.group_ctas = gc;
+        if ((s = consider(p)) != GBS_OK) return s;
+    }
+    // 2. schedule at the best shape
+    const gbs_batch_params shape = best;
+    for (int split = 0; split < 2; ++split) {
+        for (double sc : {0.5, 1.0, 2.0, 4.0, 8.0, 16.0}) {
+            if (split == 0 && sc == 1.0) continue;
+            gbs_batch_params p = shape;
+            p.delta_scale = sc;
+            p.light = split ? INFINITY : -1.0;
+            if ((s = consider(p)) != GBS_OK) return s;
+        }
+    }
+    for (uint32_t v : kInline) {
+        gbs_batch_params p = best;
+        p.inline_edges = v;
+        if ((s = consider(p)) != GBS_OK) return s;
+    }
+    out->best = best;
+    out->best_ms = best_ms;
+    return GBS_OK;
+}
+
+uint32_t batch_blocks(int device) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    return (uint32_t)std::max(1, persistent_ctas_per_sm(false, true) * sms);
+}
+
+}  // namespace
+
+extern "C" {
+
+gbs_status gbs_autotune_plan_sources(gbs_graph *g, const uint32_t *sources, uint32_t k, double budget_ms,
+                                     gbs_batch_tune_report *out) {
+    if (!g || !sources || k == 0 || !out) return fail(GBS_ERR_INVALID_ARG, "graph, sources and out are required");
+    auto make = [&](const gbs_batch_params &bp, gbs_plan **plan) {
+        return gbs_plan_sources(g, sources, k, &bp, nullptr, nullptr, plan);
+    };
+    return tune_plan(make, batch_blocks(g->device), budget_ms, out);
+}
+
+gbs_status gbs_autotune_plan_pack(gbs_pack *pk, const uint32_t *sources, double budget_ms,
+                                  gbs_batch_tune_report *out) {
+    if (!pk || !sources || !out) return fail(GBS_ERR_INVALID_ARG, "pack, sources and out are required");
+    int dev = 0;
+    GBS_CUDA(cudaGetDevice(&dev));
+    auto make = [&](const gbs_batch_params &bp, gbs_plan **plan) {
+        return gbs_plan_pack(pk, sources, &bp, nullptr, nullptr, plan);
+    };
+    return tune_plan(make, batch_blocks(dev), budget_ms, out);
+}
+
+}  // extern "C"

@@ -72,6 +72,10 @@ typedef struct gbs_params {
                                 one CTA without a grid barrier; 0 = 1024 */
     uint32_t solo_descs;     /* likewise for a relaxation of at most this many
                                 128-edge descriptors; 0 = 64 */
+    uint32_t inline_edges;   /* rows of at most this many edges are relaxed by the
+                                scanning warp, longer rows are cut into 128-edge
+                                descriptors relaxed one warp each; 0 = 32 */
+    uint32_t reserved;
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
@@ -216,7 +220,7 @@ typedef struct gbs_batch_params {
     uint32_t wait_limit_ms;
     uint32_t solo_entries;
     uint32_t solo_descs;
-    uint32_t reserved;
+    uint32_t inline_edges;   /* as gbs_params.inline_edges */
 } gbs_batch_params;
 
 /* Per-instance result record (device times from %globaltimer). */
@@ -275,6 +279,47 @@ gbs_status gbs_plan_launch(gbs_plan *plan);
  * unsolved. */
 gbs_status gbs_plan_wait(gbs_plan *plan, gbs_batch_stats *stats, gbs_inst_stats *per_instance);
 gbs_status gbs_plan_destroy(gbs_plan *plan);
+
+/*
+ * Autotuner (no counterpart in the reference, which fixes the bucket width:
+ * 0.4 in main/main.c:223, 0.1 in btwcentral/csr_bc.c:43).  Times candidate
+ * schedules on the given sources and returns the fastest.  Every schedule
+ * gives bit-identical distances and predecessors; only time changes.
+ *
+ * gbs_autotune (single source): bucket width as a multiple of the default
+ * (max weight / average out-degree), light/heavy split at delta or none,
+ * inline-row threshold, solo thresholds.  Coordinate search: the width for
+ * each split, then the other knobs one at a time around the best.
+ * gbs_autotune_plan_* (batched): CTAs per group, then the schedule.
+ * budget_ms bounds the device time spent (0 = 4000 ms); at least the default
+ * and one candidate are always timed.
+ */
+typedef struct gbs_tune_report {
+    gbs_params best;         /* fastest schedule (delta and light explicit) */
+    double best_ms;          /* its mean kernel time per source */
+    double default_ms;       /* the plain schedule: default delta, light = delta */
+    double delta_scale;      /* best delta / default delta */
+    uint32_t candidates;     /* schedules timed */
+    uint32_t runs;           /* SSSP runs made */
+    int32_t no_split;        /* 1: the best schedule has no light/heavy split */
+    uint32_t reserved;
+} gbs_tune_report;
+
+gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, double budget_ms,
+                        gbs_tune_report *out);
+
+typedef struct gbs_batch_tune_report {
+    gbs_batch_params best;
+    double best_ms;          /* device time of one launch with the best parameters */
+    double default_ms;       /* the same with group_ctas chosen by the library, default schedule */
+    uint32_t candidates;
+    uint32_t reserved;
+} gbs_batch_tune_report;
+
+gbs_status gbs_autotune_plan_sources(gbs_graph *g, const uint32_t *sources, uint32_t k, double budget_ms,
+                                     gbs_batch_tune_report *out);
+gbs_status gbs_autotune_plan_pack(gbs_pack *p, const uint32_t *sources, double budget_ms,
+                                  gbs_batch_tune_report *out);
 
 /*
  * SSSP that allocates no memory (no counterpart in the reference).  For
