@@ -46,7 +46,7 @@ __global__ void k_mid(const uint32_t *__restrict__ row, const uint2 *__restrict_
 }
 
 __global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restrict__ tag, uint32_t n,
-                        uint32_t src, uint32_t *__restrict__ ring0, Ctl *ctl) {
+                        uint32_t src, uint32_t *__restrict__ ring0, Ctl *ctl, uint32_t span0, uint32_t full0) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         dp[v] = (v == src) ? (unsigned long long)src : kUnreached;   // dist 0, pred = src
         tag[v] = (v == src) ? 0u : kTagInit;
@@ -58,6 +58,8 @@ __global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restric
         ctl->pend_min[1].v = kTagInit;
         ctl->pub_phase = kPhLightFirst;
         ctl->pub_b = 0;
+        ctl->pub_span = span0;   // bucket 0 spans span0 base widths
+        ctl->pub_full = full0;
     }
 }
 
@@ -327,6 +329,9 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.no_heavy = r.light_bits >= max_weight_bits(g->wtype, g->max_w) ? 1u : 0u;
     a.inline_max = (p && p->inline_edges) ? p->inline_edges : kInlineEdges;
     a.run_ns = a.wait_ns * 16ull;
+    a.ctrl = kCtrlFixed;
+    a.span_fixed = 1;
+    const uint32_t span0 = 1, full0 = a.no_heavy;
     a.group = 0;
     a.group_ctas = (uint32_t)g->blocks;
     a.ws.n_cap = g->n;
@@ -340,7 +345,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
 
     GBS_CUDA(cudaEventRecord(g->ev[0], s));
     GBS_CUDA(cudaMemsetAsync(g->ws.ctl, 0, sizeof(Ctl), s));
-    k_reset<<<eb, tb, 0, s>>>(g->ws.dp, g->ws.tag, g->n, src, g->ws.ring, g->ws.ctl);
+    k_reset<<<eb, tb, 0, s>>>(g->ws.dp, g->ws.tag, g->n, src, g->ws.ring, g->ws.ctl, span0, full0);
     GBS_CUDA(cudaGetLastError());
     GBS_CUDA(cudaEventRecord(g->ev[1], s));
     void *args[] = {&a};

@@ -41,7 +41,28 @@ enum ErrCode : uint32_t {
     kErrTimeout = 1,
     kErrCapacity = 2,
     kErrOverflow = 3,
+    kErrGuard = 4,          // the learned schedule ran past its time guard (host reruns the plain one)
 };
+
+// Bucket-width controller of a run.
+enum CtrlMode : uint32_t {
+    kCtrlFixed = 0,         // every bucket spans span_fixed base widths, split as no_heavy says
+    kCtrlLearned = 1,       // the MLP picks span and split at every bucket start
+};
+
+constexpr int kFeat = 16;           // controller features
+constexpr int kHid = 64;            // hidden units of each of the two layers
+// Parameter block of the controller, floats:
+//   mu[16] sd[16] W1[16][64] b1[64] W2[64][64] b2[64] W3[64][2] b3[2]
+constexpr int kMlpW1 = 2 * kFeat;
+constexpr int kMlpB1 = kMlpW1 + kFeat * kHid;
+constexpr int kMlpW2 = kMlpB1 + kHid;
+constexpr int kMlpB2 = kMlpW2 + kHid * kHid;
+constexpr int kMlpW3 = kMlpB2 + kHid;
+constexpr int kMlpB3 = kMlpW3 + kHid * 2;
+constexpr int kMlpFloats = kMlpB3 + 2;
+constexpr int kMlpParams = kMlpFloats - 2 * kFeat;   // trained parameters (5,378)
+constexpr uint32_t kMaxSpanLog = 6;                  // a bucket spans at most 2^6 = kNB base widths
 
 // One record per grid phase when GBS_F_TRACE is set (layout = gbs_phase_rec).
 struct TraceRec {
@@ -81,7 +102,10 @@ struct __align__(128) Ctl {
     uint32_t pub_hround;
     uint32_t pub_pend_sel;
     uint32_t pub_inst;            // instance being solved (batched launches)
-    uint32_t pad2[22];
+    uint32_t pub_span;            // base widths the current bucket spans
+    uint32_t pub_full;            // 1: light scans relax whole rows, no heavy scan
+    uint32_t feat_n;              // feature vectors recorded
+    uint32_t pad2[19];
     Line ring_cnt[kNB];
     Line fq_cnt[3];
     Line s_cnt[2];
@@ -101,6 +125,7 @@ struct __align__(128) Ctl {
     unsigned long long st_edges_reached;
     unsigned long long inst_t0;   // globaltimer when the current instance started
 };
+static_assert(sizeof(Ctl) % 128 == 0, "Ctl lines");
 
 struct DevGraph {
     uint32_t n;
@@ -171,6 +196,15 @@ struct SsspArgs {
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
     uint32_t no_heavy;      // the split covers every edge: light scans relax whole rows, no HEAVY phase
     uint32_t inline_max;    // rows up to this long are relaxed by the scanning warp
+    // bucket-width controller
+    uint32_t ctrl;          // CtrlMode
+    uint32_t span_fixed;    // kCtrlFixed: base widths per bucket (0 or 1 = plain delta-stepping)
+    float span_bias;        // kCtrlLearned: span = 2^clamp(round(y0 + span_bias), 0, kMaxSpanLog)
+    const float *mlp;       // kCtrlLearned: parameter block (kMlpFloats)
+    float gfeat[5];         // graph features 11..15 of the controller input
+    unsigned long long guard_ns;   // kCtrlLearned: stop with kErrGuard past this run time (0 = none)
+    float *feat;            // GBS_F_FEATURES: kFeat floats per bucket start
+    uint32_t feat_cap;
     uint32_t group;         // this CTA's group and the CTAs in one group
     uint32_t group_ctas;
     uint32_t *dist_out;     // batched: the current instance's outputs

@@ -93,6 +93,8 @@ __global__ void k_noalloc_reset(unsigned long long *__restrict__ dp, uint32_t *_
         ctl->pend_min[1].v = kTagInit;
         ctl->pub_phase = kPhLightFirst;
         ctl->pub_b = 0;
+        ctl->pub_span = 1;   // plain delta-stepping, no split (every edge light)
+        ctl->pub_full = 1;
     }
 }
 
@@ -234,6 +236,8 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.solo_desc = 64;
     a.no_heavy = 1;  // every edge is light (see mid above)
     a.inline_max = kInlineEdges;
+    a.ctrl = kCtrlFixed;
+    a.span_fixed = 1;
     a.wait_ns = 4000ull * 1000000ull;
     a.run_ns = a.wait_ns * 16ull;
     a.group = 0;

@@ -50,9 +50,11 @@ __device__ __forceinline__ Exec cta_exec() {
 // ------------------------------------------------------------------- SCAN
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
+// A light scan relaxes the row prefix [row, mid), or the whole row when full;
+// a heavy scan the rest [mid, end).
 template <bool F32>
 __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x, const uint32_t *F,
-                              uint32_t count, uint32_t vtag, bool light, bool add_s, uint32_t hround,
+                              uint32_t count, uint32_t vtag, bool light, bool full, bool add_s, uint32_t hround,
                               uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
@@ -69,7 +71,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             // the tag check and the row reads are independent: issue together
             const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
             du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
-            const uint32_t md = __ldg(a.ws.mid + u);
+            const uint32_t md = full ? __ldg(a.g.row + u + 1) : __ldg(a.ws.mid + u);
             const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
             ok = tg == vtag;
             s = ok ? (light ? r : md) : 0u;
@@ -246,27 +248,33 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     Ctl *ctl = a.ws.ctl;
     const uint32_t n = a.g.n;
     Targets t;
-    t.cur_hi = U.b + 1;
+    t.cur_hi = U.b + U.span;   // the bucket covers base buckets [b, b + span)
     t.W = U.W;
     t.stamp_next = U.epoch + 1;
     t.fq_next = (U.epoch + 1) % 3u;
     t.pend_sel = U.pend_sel;
     t.scr = scr;
+    const bool full = U.full != 0;
     switch (U.phase) {
         case kPhLightFirst:
-            scan_frontier<F32>(a, t, x, a.ws.ring + (size_t)(U.b % kNB) * n,
-                               min(__ldcg(&ctl->ring_cnt[U.b % kNB].v), n), U.b, true, !a.no_heavy, U.hround,
-                               imp);
+            // the ring lists of every base bucket the bucket spans, one after
+            // the other (independent: no barrier between them)
+            for (uint32_t j = 0; j < U.span; ++j) {
+                const uint32_t bk = U.b + j;
+                scan_frontier<F32>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n,
+                                   min(__ldcg(&ctl->ring_cnt[bk % kNB].v), n), bk, true, full, !full, U.hround,
+                                   imp);
+            }
             break;
         case kPhLight:
             scan_frontier<F32>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, !a.no_heavy,
+                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, full, !full,
                                U.hround, imp);
             break;
         case kPhHeavy:
             scan_frontier<F32>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
-                               min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), n), kTagInit, false, false, U.hround,
-                               imp);
+                               min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), n), kTagInit, false, false, false,
+                               U.hround, imp);
             break;
         case kPhEdges:
             relax_descriptors<F32>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
@@ -287,6 +295,36 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
 
 __device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
     return phase == kPhHeavy ? (uint32_t)kPhHeavy : (uint32_t)kPhLight;
+}
+
+// Span and split of the bucket that starts at base bucket nb, and the entries
+// of the lists it spans (warp-collective: warp 0 of the deciding CTA).
+__device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint32_t nb, uint32_t lim,
+                                              uint32_t ring_lo, uint32_t ring_hi, uint32_t pend, uint32_t pm,
+                                              uint32_t &span_out, uint32_t &full_out, uint32_t &first_items) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    auto ring_count = [&](uint32_t bucket) {
+        const uint32_t slot = bucket % kNB;
+        const uint32_t lo = __shfl_sync(FULL, ring_lo, slot & 31u);
+        const uint32_t hi = __shfl_sync(FULL, ring_hi, slot & 31u);
+        return slot < 32 ? lo : hi;
+    };
+    // occupancy of the base buckets from nb on (inside the window only)
+    uint32_t c_lo = ring_count(nb + lane), c_hi = ring_count(nb + 32u + lane);
+    c_lo = (nb + lane < lim) ? c_lo : 0u;
+    c_hi = (nb + 32u + lane < lim) ? c_hi : 0u;
+    uint32_t span = a.span_fixed ? a.span_fixed : 1u;
+    uint32_t full = a.no_heavy;
+    // a bucket never reaches past the smallest pending bucket
+    while (span > 1u && pend > 0u && nb + span > pm) span >>= 1;
+    span_out = span;
+    full_out = full;
+    // entries of the span's lists (for the solo decision)
+    uint32_t cnt = (lane < span ? c_lo : 0u) + (lane + 32u < span ? c_hi : 0u);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
+    first_items = cnt;
 }
 
 // The uniform state after the decision (identical in every CTA that adopts it).
@@ -336,7 +374,14 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         const uint32_t hi = __shfl_sync(FULL, ring_hi, slot & 31u);
         return slot < 32 ? lo : hi;
     };
-    const uint32_t cur_ring = ring_count(U.b);
+    // entries of the lists the current bucket spans (trace)
+    uint32_t cur_ring;
+    {
+        const uint32_t c1 = ring_count(U.b + lane), c2 = ring_count(U.b + 32u + lane);
+        cur_ring = (lane < U.span ? c1 : 0u) + (lane + 32u < U.span ? c2 : 0u);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cur_ring += __shfl_xor_sync(FULL, cur_ring, o);
+    }
 
     uint32_t next = kPhDone, nb = 0;
     uint32_t ps2 = U.pend_sel;
@@ -361,17 +406,17 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
         if (fq_next > 0) {
             next = kPhLight;
-        } else if (logical == kPhLight && !a.no_heavy) {
+        } else if (logical == kPhLight && !U.full) {
             next = kPhHeavy;
         } else {
             bucket_end = true;
             need_ring_scan = true;
-            scan_from = U.b + 1;
+            scan_from = U.b + U.span;
         }
     }
     if (need_ring_scan) {
         // first non-empty ring bucket in [scan_from, W + kNB); at a bucket end
-        // scan_from = b + 1 = W + 1, so the slot being cleared is not read.
+        // scan_from = b + span = W + span, so the slots being cleared are not read.
         const uint32_t lim = U.W + kNB;   // exclusive
         uint32_t found = 0xFFFFFFFFu;
 #pragma unroll
@@ -417,10 +462,18 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             N.hround = 1u;
         }
     }
+    uint32_t first_items = 0;   // LIGHT_FIRST: entries of every list the new bucket spans
+    if (next == kPhLightFirst) {
+        uint32_t span, full;
+        decide_bucket(a, ctl, nb, U.W + kNB, ring_lo, ring_hi, ps2 ? pc1 : pc0, ps2 ? pm1 : pm0, span, full,
+                      first_items);
+        N.span = span;
+        N.full = full;
+    }
     // size of the next phase's input
     uint32_t items = 0;
     switch (next) {
-        case kPhLightFirst: items = ring_count(nb); break;
+        case kPhLightFirst: items = first_items; break;
         case kPhLight: items = fq_next; break;
         case kPhHeavy: items = s_cur; break;
         case kPhEdges: items = desc_cnt; break;
@@ -445,7 +498,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
                     default: done_items = U.pend_sel ? pc1 : pc0; break;
                 }
                 TraceRec r;
-                r.kind = U.phase | (was_solo ? 16u : 0u);
+                r.kind = U.phase | (was_solo ? 16u : 0u) | (U.span << 8) | (U.full << 16);
                 r.bucket = U.b;
                 r.items = done_items;
                 r.edges = edge_cnt;
@@ -482,7 +535,6 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         }
         if (was_solo) ctl->st_solo_phases += 1;
         if (next == kPhPending) ctl->edge_cnt.v = 0;   // counts stale entries there
-        if (bucket_end) ctl->ring_cnt[U.b % kNB].v = 0;
         if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
             ctl->fq_cnt[(N.epoch + 1u) % 3u].v = 0;
             ctl->desc_cnt.v = 0;
@@ -497,6 +549,12 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         ctl->pub_hround = N.hround;
         ctl->pub_pend_sel = N.pend_sel;
         ctl->pub_inst = N.inst;
+        ctl->pub_span = N.span;
+        ctl->pub_full = N.full;
+    }
+    if (bucket_end) {   // the lists of the finished bucket
+        if (lane < U.span) ctl->ring_cnt[(U.b + lane) % kNB].v = 0u;
+        if (lane + 32u < U.span) ctl->ring_cnt[(U.b + 32u + lane) % kNB].v = 0u;
     }
     if (take && next == kPhInit) {
         // every list of the new instance starts empty; the source waits in
@@ -539,6 +597,8 @@ __device__ __forceinline__ void fetch_published(Ctl *ctl, uint32_t *s_pub) {
     s_pub[5] = ld_relaxed(&ctl->pub_hround);
     s_pub[6] = ld_relaxed(&ctl->pub_pend_sel);
     s_pub[7] = ld_relaxed(&ctl->pub_inst);
+    s_pub[8] = ld_relaxed(&ctl->pub_span);
+    s_pub[9] = ld_relaxed(&ctl->pub_full);
 }
 
 __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &U) {
@@ -550,6 +610,8 @@ __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &
     U.hround = s_pub[5];
     U.pend_sel = s_pub[6];
     U.inst = s_pub[7];
+    U.span = s_pub[8];
+    U.full = s_pub[9];
 }
 
 // Grid barrier after a phase.  The CTA that arrives last decides the next
@@ -563,7 +625,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
                                                    uint32_t &imp) {
     Ctl *ctl = a.ws.ctl;
     __shared__ uint32_t s_flag[2];
-    __shared__ uint32_t s_pub[8];
+    __shared__ uint32_t s_pub[10];
     __syncthreads();
     if (threadIdx.x == 0) {
         // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
@@ -645,6 +707,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     U.hround = a.hround0;
     U.pend_sel = 0;
     U.inst = kNoInst;
+    U.span = ld_relaxed(&ctl->pub_span);
+    U.full = ld_relaxed(&ctl->pub_full);
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t imp = 0;
@@ -685,6 +749,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Works
     U.hround = ld_relaxed(&ctl->next_hround);
     U.pend_sel = 0;
     U.inst = kNoInst;
+    U.span = 1;
+    U.full = 0;
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t loaded = kNoInst;
