@@ -39,6 +39,9 @@ EXPORTS = [
     "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
     "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
     "gbs_autotune", "gbs_autotune_plan_sources", "gbs_autotune_plan_pack",
+    "gbs_graph_set_controller", "gbs_features", "gbs_mlp_create", "gbs_mlp_destroy", "gbs_mlp_set_params",
+    "gbs_mlp_get_params", "gbs_mlp_set_data", "gbs_mlp_loss_grad", "gbs_mlp_adam", "gbs_mlp_train",
+    "gbs_mlp_predict",
     "gbs_device_alloc", "gbs_device_free",
     "gbs_device_synchronize", "gbs_memcpy",
     "gbs_gen_rmat", "gbs_gen_grid", "gbs_sample_sources", "gbs_host_csr_free",
@@ -68,6 +71,11 @@ class PhaseRec(ctypes.Structure):
 PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "scan_heavy", 3: "relax", 4: "pending"}
 F_TRACE = 0x2
 F_NO_SOLO = 0x4
+F_FEATURES = 0x8
+F_LEARNED = 0x10
+N_FEAT = 16
+MLP_FLOATS = 5410      # controller block: means, scales, W1, b1, W2, b2, W3, b3
+MLP_PARAMS = 5378      # the trained part
 F_TEST_STALL = 0x80000000
 
 
@@ -78,7 +86,7 @@ class Stats(ctypes.Structure):
                 ("phases", ctypes.c_uint32), ("pending_scans", ctypes.c_uint32),
                 ("blocks", ctypes.c_uint32), ("delta_used", ctypes.c_double),
                 ("light_used", ctypes.c_double), ("solo_phases", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("learned", ctypes.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -177,6 +185,17 @@ def _load() -> ctypes.CDLL:
     L.gbs_plan_wait.argtypes = [P, ctypes.POINTER(BatchStats), P]
     L.gbs_plan_destroy.argtypes = [P]
     L.gbs_autotune.argtypes = [P, P, ctypes.c_uint32, ctypes.c_double, ctypes.POINTER(TuneReport)]
+    L.gbs_graph_set_controller.argtypes = [P, P, ctypes.c_uint32, ctypes.c_double]
+    L.gbs_features.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+    L.gbs_mlp_create.argtypes = [ctypes.POINTER(P)]
+    L.gbs_mlp_destroy.argtypes = [P]
+    L.gbs_mlp_set_params.argtypes = [P, P]
+    L.gbs_mlp_get_params.argtypes = [P, P]
+    L.gbs_mlp_set_data.argtypes = [P, P, P, P, ctypes.c_uint32]
+    L.gbs_mlp_loss_grad.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), P]
+    L.gbs_mlp_adam.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+    L.gbs_mlp_train.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64, P]
+    L.gbs_mlp_predict.argtypes = [P, P, ctypes.c_uint32, P]
     L.gbs_autotune_plan_sources.argtypes = [P, P, ctypes.c_uint32, ctypes.c_double,
                                             ctypes.POINTER(BatchTuneReport)]
     L.gbs_autotune_plan_pack.argtypes = [P, P, ctypes.c_double, ctypes.POINTER(BatchTuneReport)]
@@ -388,9 +407,29 @@ class Graph:
         recs = (PhaseRec * max(1, cnt.value))()
         _check(lib.gbs_trace(self._h, recs, cnt.value, ctypes.byref(cnt)), "gbs_trace")
         return [{"kind": PHASE_KINDS.get(r.kind & 15, r.kind), "solo": bool(r.kind & 16),
+                 "span": (r.kind >> 8) & 0xFF, "full": bool((r.kind >> 16) & 1),
                  "bucket": r.bucket, "items": r.items, "edges": r.edges, "pending": r.pending,
                  "window": r.window, "end_ns": r.end_ns}
                 for r in recs[: cnt.value]]
+
+    def set_controller(self, params: np.ndarray | None, margin: float = 0.0) -> None:
+        """Installs the learned bucket-width controller (MLP_FLOATS float32
+        values) used by runs with flags=F_LEARNED; None removes it."""
+        if params is None:
+            _check(lib.gbs_graph_set_controller(self._h, None, 0, 0.0), "gbs_graph_set_controller")
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib.gbs_graph_set_controller(self._h, _ptr(p), len(p), float(margin)), "gbs_graph_set_controller")
+
+    def features(self) -> np.ndarray:
+        """Controller inputs recorded by the last run made with F_FEATURES
+        (one row of N_FEAT per bucket start)."""
+        cnt = ctypes.c_uint32()
+        _check(lib.gbs_features(self._h, None, 0, ctypes.byref(cnt)), "gbs_features")
+        out = np.empty((cnt.value, N_FEAT), dtype=np.float32)
+        if cnt.value:
+            _check(lib.gbs_features(self._h, _ptr(out), cnt.value, ctypes.byref(cnt)), "gbs_features")
+        return out
 
     def sssp(self, source: int, delta: float | None = None, light: float | None = None,
              out_dist: np.ndarray | None = None, out_pred: np.ndarray | None = None,
@@ -654,3 +693,68 @@ def autotune_plan(target, sources, budget_ms: float = 0.0):
     r = {"best_ms": rep.best_ms, "default_ms": rep.default_ms, "candidates": rep.candidates,
          "best": _struct_dict(best)}
     return best, r
+
+
+# ---------------------------------------------------- controller training
+class Mlp:
+    """The controller network on the GPU (gbs_mlp): parameters, gradient,
+    Adam state and a training set, with the library's CUDA kernels."""
+
+    def __init__(self, params: np.ndarray | None = None):
+        h = ctypes.c_void_p()
+        _check(lib.gbs_mlp_create(ctypes.byref(h)), "gbs_mlp_create")
+        self._h = h
+        self.n = 0
+        if params is not None:
+            self.set_params(params)
+
+    def set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.shape == (MLP_FLOATS,)
+        _check(lib.gbs_mlp_set_params(self._h, _ptr(p)), "gbs_mlp_set_params")
+
+    def params(self) -> np.ndarray:
+        p = np.empty(MLP_FLOATS, dtype=np.float32)
+        _check(lib.gbs_mlp_get_params(self._h, _ptr(p)), "gbs_mlp_get_params")
+        return p
+
+    def set_data(self, x: np.ndarray, t: np.ndarray, w: np.ndarray | None = None) -> None:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        assert x.ndim == 2 and x.shape[1] == N_FEAT and t.shape == (len(x), 2)
+        self.n = len(x)
+        _check(lib.gbs_mlp_set_data(self._h, _ptr(x), _ptr(t), _ptr(w) if w is not None else None, len(x)),
+               "gbs_mlp_set_data")
+
+    def loss_grad(self, first: int = 0, count: int | None = None):
+        count = self.n - first if count is None else count
+        loss = ctypes.c_double()
+        g = np.empty(MLP_PARAMS, dtype=np.float32)
+        _check(lib.gbs_mlp_loss_grad(self._h, first, count, ctypes.byref(loss), _ptr(g)), "gbs_mlp_loss_grad")
+        return loss.value, g
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> None:
+        _check(lib.gbs_mlp_adam(self._h, lr, beta1, beta2, eps), "gbs_mlp_adam")
+
+    def train(self, epochs: int, batch: int, lr: float, seed: int = 0) -> np.ndarray:
+        losses = np.zeros(epochs, dtype=np.float64)
+        _check(lib.gbs_mlp_train(self._h, epochs, batch, lr, seed, _ptr(losses)), "gbs_mlp_train")
+        return losses
+
+    def predict(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((len(x), 2), dtype=np.float32)
+        _check(lib.gbs_mlp_predict(self._h, _ptr(x), len(x), _ptr(y)), "gbs_mlp_predict")
+        return y
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.gbs_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -238,6 +238,8 @@ void free_graph(gbs_graph *g) {
     free_workspace(g->ws);
     cudaFree(g->d_dist);
     cudaFree(g->d_pred);
+    cudaFree(g->d_mlp);
+    cudaFree(g->d_feat);
     for (auto &e : g->ev) if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
@@ -288,12 +290,73 @@ Resolved resolve_schedule(gbs_weight_type wt, double max_w, uint32_t n, uint64_t
     return r;
 }
 
+// The controller network on the host (first prediction of a learned run).
+float mlp_host(const float *P, const float (&x)[kFeat], float &y1) {
+    float xn[kFeat], h1[kHid], h2[kHid];
+    for (int i = 0; i < kFeat; ++i) xn[i] = (x[i] - P[i]) / P[kFeat + i];
+    for (int o = 0; o < kHid; ++o) {
+        float acc = P[kMlpB1 + o];
+        for (int i = 0; i < kFeat; ++i) acc = std::fma(xn[i], P[kMlpW1 + i * kHid + o], acc);
+        h1[o] = std::max(acc, 0.f);
+    }
+    for (int o = 0; o < kHid; ++o) {
+        float acc = P[kMlpB2 + o];
+        for (int i = 0; i < kHid; ++i) acc = std::fma(h1[i], P[kMlpW2 + i * kHid + o], acc);
+        h2[o] = std::max(acc, 0.f);
+    }
+    float y0 = P[kMlpB3], y = P[kMlpB3 + 1];
+    for (int o = 0; o < kHid; ++o) {
+        y0 += h2[o] * P[kMlpW3 + 2 * o];
+        y += h2[o] * P[kMlpW3 + 2 * o + 1];
+    }
+    y1 = y;
+    return y0;
+}
+
+// Graph features 11..14 of the controller input (15 is set per run).
+void graph_features(const gbs_graph *g, float *f) {
+    const double avg = g->n ? (double)g->m / (double)g->n : 0.0;
+    f[0] = (float)std::log2((double)std::max<uint32_t>(g->n, 1));
+    f[1] = (float)std::log2(std::max(avg, 1e-3));
+    f[2] = (float)std::log2(std::max(g->max_w, 1e-30));
+    f[3] = g->max_w > 0 ? (float)(g->mean_w / g->max_w) : 0.f;
+}
+
 gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t *dist_dev,
-                      int32_t *pred_dev, gbs_stats *stats) {
+                      int32_t *pred_dev, gbs_stats *stats, bool learned, bool *guard_hit) {
     if (src >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
+    if (guard_hit) *guard_hit = false;
     gbs_status st = ensure_workspace(g);
     if (st != GBS_OK) return st;
-    const Resolved r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, p ? p->delta : 0.0, p ? p->light : -1.0);
+    const double d_def = default_delta(g->max_w, g->n, g->m);
+    Resolved r;
+    float gfeat[5];
+    graph_features(g, gfeat);
+    float span_bias = 0.f;
+    uint32_t span0 = 1, full0 = 0;
+    if (learned) {
+        // the controller's first prediction (bucket 0 holds only the source)
+        // fixes the base width: 1/8 of the predicted delta, so spans of 1..64
+        // base widths reach 8x below and 8x above it; the split is at the
+        // predicted delta
+        float x[kFeat];
+        for (int i = 0; i < 7; ++i) x[i] = 1.f;
+        for (int i = 7; i < 11; ++i) x[i] = 0.f;
+        for (int i = 0; i < 4; ++i) x[11 + i] = gfeat[i];
+        x[15] = 0.f;
+        float y1 = 0.f;
+        const float y0 = mlp_host(g->mlp_host.data(), x, y1);
+        const double p0 = std::rint(std::min(std::max((double)y0, -20.0), 30.0));
+        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 3.0), d_def * std::exp2(p0));
+        span_bias = (float)std::log2(d_def / r.delta);
+        int e0 = (int)std::rint(y0 + span_bias);
+        e0 = std::min(std::max(e0, 0), (int)kMaxSpanLog);
+        span0 = 1u << e0;
+        full0 = y1 <= 0.f ? 1u : 0u;
+    } else {
+        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, p ? p->delta : 0.0, p ? p->light : -1.0);
+    }
+    gfeat[4] = (float)std::log2(r.delta / d_def);
     cudaStream_t s = g->stream;
     const int tb = 256;
     const int eb = std::max(1, std::min<int>((g->n + tb - 1) / tb, g->sms * 8));
@@ -329,9 +392,23 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.no_heavy = r.light_bits >= max_weight_bits(g->wtype, g->max_w) ? 1u : 0u;
     a.inline_max = (p && p->inline_edges) ? p->inline_edges : kInlineEdges;
     a.run_ns = a.wait_ns * 16ull;
-    a.ctrl = kCtrlFixed;
+    a.ctrl = learned ? kCtrlLearned : kCtrlFixed;
     a.span_fixed = 1;
-    const uint32_t span0 = 1, full0 = a.no_heavy;
+    a.span_bias = span_bias;
+    a.mlp = learned ? g->d_mlp : nullptr;
+    for (int i = 0; i < 5; ++i) a.gfeat[i] = gfeat[i];
+    a.guard_ns = (learned && g->plain_ms > 0)
+                     ? (unsigned long long)(g->plain_ms * (1.0 + g->ctrl_margin) * 1e6)
+                     : 0ull;
+    if (!learned || a.no_heavy) full0 = a.no_heavy;
+    if (a.flags & GBS_F_FEATURES) {
+        if (!g->d_feat) {
+            g->feat_cap = 1u << 18;
+            GBS_CUDA(cudaMalloc(&g->d_feat, sizeof(float) * kFeat * g->feat_cap));
+        }
+        a.feat = g->d_feat;
+        a.feat_cap = g->feat_cap;
+    }
     a.group = 0;
     a.group_ctas = (uint32_t)g->blocks;
     a.ws.n_cap = g->n;
@@ -372,9 +449,14 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     g->epoch = c.next_epoch + 1;
     g->hround = c.next_hround + 1;
     g->trace_n = (a.flags & GBS_F_TRACE) ? std::min(c.trace_n, g->ws.trace_cap) : 0u;
+    g->feat_n = (a.flags & GBS_F_FEATURES) ? std::min(c.feat_n, g->feat_cap) : 0u;
     if (c.error != kErrNone) {
         // stamps of an aborted run are unknown: start over next time
         g->epoch = 0xF0000001u;
+        if (c.error == kErrGuard && guard_hit) {
+            *guard_hit = true;
+            return GBS_OK;
+        }
         switch (c.error) {
             case kErrTimeout: return fail(GBS_ERR_TIMEOUT, "device-side wait limit exceeded");
             case kErrCapacity: return fail(GBS_ERR_CAPACITY, "device work list overflow");
@@ -399,7 +481,40 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
         stats->solo_phases = c.st_solo_phases;
         stats->delta_used = r.delta;
         stats->light_used = r.light;
+        stats->learned = learned ? 1u : 0u;
     }
+    return GBS_OK;
+}
+
+// One SSSP with the schedule the flags ask for.  GBS_F_LEARNED: the first
+// learned run on a graph is preceded by a plain run that times the plain
+// schedule; a learned run that passes (1 + margin) x that time stops and the
+// plain schedule runs instead.
+gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t *dist_dev, int32_t *pred_dev,
+                    gbs_stats *stats) {
+    const bool learned = p && (p->flags & GBS_F_LEARNED);
+    if (!learned) return launch_run(g, src, p, dist_dev, pred_dev, stats, false, nullptr);
+    if (!g->d_mlp) return fail(GBS_ERR_INVALID_ARG, "GBS_F_LEARNED: no controller set (gbs_graph_set_controller)");
+    gbs_params plain = *p;
+    plain.flags &= ~GBS_F_LEARNED;
+    plain.delta = 0.0;    // the plain heuristic: max weight / average out-degree
+    plain.light = -1.0;   // light = delta
+    gbs_stats ps;
+    gbs_status st;
+    if (!(g->plain_ms > 0)) {
+        st = launch_run(g, src, &plain, nullptr, nullptr, &ps, false, nullptr);
+        if (st != GBS_OK) return st;
+        g->plain_ms = ps.kernel_ms;
+    }
+    bool guard = false;
+    st = launch_run(g, src, p, dist_dev, pred_dev, stats, true, &guard);
+    if (st != GBS_OK || !guard) return st;
+    gbs_stats rs;
+    st = launch_run(g, src, &plain, dist_dev, pred_dev, &rs, false, nullptr);
+    if (st != GBS_OK) return st;
+    g->plain_ms = std::max(g->plain_ms, rs.kernel_ms);
+    rs.learned = 3u;
+    if (stats) *stats = rs;
     return GBS_OK;
 }
 
@@ -448,6 +563,9 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
     double max_w = 0.0;
     gbs_status st = prepare_csr(n, m, row_offsets, cols, weights, wtype, row32, adj, max_w);
     if (st != GBS_OK) return st;
+    double wsum = 0.0;
+    for (uint64_t e = 0; e < m; ++e)
+        wsum += wtype == GBS_WEIGHT_U32 ? (double)((const uint32_t *)weights)[e] : (double)((const float *)weights)[e];
     int dev = 0;
     GBS_CUDA(cudaGetDevice(&dev));
     gbs_graph *g = new gbs_graph();
@@ -455,6 +573,7 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
     g->m = m;
     g->wtype = wtype;
     g->max_w = max_w;
+    g->mean_w = m ? wsum / (double)m : 0.0;
     g->device = dev;
     cudaError_t e;
     if ((e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
@@ -502,7 +621,7 @@ gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m, gbs_weig
 gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_dev,
                            int32_t *pred_dev, gbs_stats *stats) {
     if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
-    return launch_run(g, source, params, (uint32_t *)dist_dev, pred_dev, stats);
+    return run_sssp(g, source, params, (uint32_t *)dist_dev, pred_dev, stats);
 }
 
 gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_out,
@@ -510,7 +629,7 @@ gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, voi
     if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
     gbs_status st = ensure_workspace(g);
     if (st != GBS_OK) return st;
-    st = launch_run(g, source, params, dist_out ? g->d_dist : nullptr, pred_out ? g->d_pred : nullptr,
+    st = run_sssp(g, source, params, dist_out ? g->d_dist : nullptr, pred_out ? g->d_pred : nullptr,
                     stats);
     if (st != GBS_OK) return st;
     if (dist_out)
@@ -546,6 +665,33 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k, con
         total.light_used = one.light_used;
     }
     if (stats) *stats = total;
+    return GBS_OK;
+}
+
+gbs_status gbs_graph_set_controller(gbs_graph *g, const float *params, uint32_t count, double margin) {
+    if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    if (!params) {   // back to no controller
+        cudaFree(g->d_mlp);
+        g->d_mlp = nullptr;
+        g->mlp_host.clear();
+        return GBS_OK;
+    }
+    if (count != (uint32_t)kMlpFloats) return fail(GBS_ERR_INVALID_ARG, "controller block must hold 5410 floats");
+    for (int i = 0; i < kFeat; ++i)
+        if (!(params[kFeat + i] > 0.f)) return fail(GBS_ERR_INVALID_ARG, "controller: input scales must be > 0");
+    if (!g->d_mlp) GBS_CUDA(cudaMalloc(&g->d_mlp, sizeof(float) * kMlpFloats));
+    GBS_CUDA(cudaMemcpy(g->d_mlp, params, sizeof(float) * kMlpFloats, cudaMemcpyHostToDevice));
+    g->mlp_host.assign(params, params + kMlpFloats);
+    g->ctrl_margin = margin > 0 ? margin : 0.25;
+    g->plain_ms = 0.0;
+    return GBS_OK;
+}
+
+gbs_status gbs_features(gbs_graph *g, float *out, uint32_t cap, uint32_t *count) {
+    if (!g || !count) return fail(GBS_ERR_INVALID_ARG, "NULL argument");
+    *count = g->feat_n;
+    const uint32_t k = std::min(cap, g->feat_n);
+    if (k && out) GBS_CUDA(cudaMemcpy(out, g->d_feat, sizeof(float) * kFeat * k, cudaMemcpyDeviceToHost));
     return GBS_OK;
 }
 

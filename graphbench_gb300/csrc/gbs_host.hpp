@@ -50,6 +50,15 @@ struct gbs_graph {
     uint32_t trace_n = 0;
     int blocks = 0;
     gbs::Ctl host_ctl{};
+    double mean_w = 0.0;
+    // learned bucket-width controller (gbs_graph_set_controller)
+    float *d_mlp = nullptr;
+    std::vector<float> mlp_host;
+    double ctrl_margin = 0.25;
+    double plain_ms = 0.0;        // kernel time of the plain schedule on this graph (the guard)
+    // recorded controller inputs (GBS_F_FEATURES)
+    float *d_feat = nullptr;
+    uint32_t feat_cap = 0, feat_n = 0;
 };
 
 namespace gbs {

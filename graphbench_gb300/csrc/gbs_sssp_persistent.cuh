@@ -297,8 +297,57 @@ __device__ __forceinline__ uint32_t scan_kind(uint32_t phase) {
     return phase == kPhHeavy ? (uint32_t)kPhHeavy : (uint32_t)kPhLight;
 }
 
+// ------------------------------------------------------------ controller
+// FP32 MLP kFeat -> kHid -> kHid -> 2 (ReLU), parameter block laid out as
+// kMlp* says; inputs are standardised with the block's mu / sd.  Warp-
+// collective: x is identical in every lane, y0 / y1 come back in every lane.
+// Lane l owns hidden units l and l + 32 of each layer.
+__device__ __forceinline__ void mlp_eval(const float *__restrict__ P, const float (&x)[kFeat], float &y0,
+                                         float &y1) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned l = lane_id();
+    float xn[kFeat];
+#pragma unroll
+    for (int i = 0; i < kFeat; ++i) xn[i] = (x[i] - __ldg(P + i)) / __ldg(P + kFeat + i);
+    float ha = __ldg(P + kMlpB1 + l), hb = __ldg(P + kMlpB1 + 32 + l);
+#pragma unroll
+    for (int i = 0; i < kFeat; ++i) {
+        ha = fmaf(xn[i], __ldg(P + kMlpW1 + i * kHid + l), ha);
+        hb = fmaf(xn[i], __ldg(P + kMlpW1 + i * kHid + 32 + l), hb);
+    }
+    ha = fmaxf(ha, 0.f);
+    hb = fmaxf(hb, 0.f);
+    float ga = __ldg(P + kMlpB2 + l), gb = __ldg(P + kMlpB2 + 32 + l);
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+        const float hi = __shfl_sync(FULL, ha, i);
+        ga = fmaf(hi, __ldg(P + kMlpW2 + i * kHid + l), ga);
+        gb = fmaf(hi, __ldg(P + kMlpW2 + i * kHid + 32 + l), gb);
+    }
+#pragma unroll 8
+    for (int i = 0; i < 32; ++i) {
+        const float hi = __shfl_sync(FULL, hb, i);
+        ga = fmaf(hi, __ldg(P + kMlpW2 + (32 + i) * kHid + l), ga);
+        gb = fmaf(hi, __ldg(P + kMlpW2 + (32 + i) * kHid + 32 + l), gb);
+    }
+    ga = fmaxf(ga, 0.f);
+    gb = fmaxf(gb, 0.f);
+    float p0 = ga * __ldg(P + kMlpW3 + 2 * l) + gb * __ldg(P + kMlpW3 + 2 * (32 + l));
+    float p1 = ga * __ldg(P + kMlpW3 + 2 * l + 1) + gb * __ldg(P + kMlpW3 + 2 * (32 + l) + 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        p0 += __shfl_xor_sync(FULL, p0, o);
+        p1 += __shfl_xor_sync(FULL, p1, o);
+    }
+    y0 = p0 + __ldg(P + kMlpB3);
+    y1 = p1 + __ldg(P + kMlpB3 + 1);
+}
+
 // Span and split of the bucket that starts at base bucket nb, and the entries
-// of the lists it spans (warp-collective: warp 0 of the deciding CTA).
+// of the lists it spans (warp-collective: warp 0 of the deciding CTA).  The
+// fixed schedule keeps span_fixed base widths; the learned one evaluates the
+// controller on the occupancy of the next base buckets, the run so far and
+// the graph.  GBS_F_FEATURES records the controller input.
 __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint32_t nb, uint32_t lim,
                                               uint32_t ring_lo, uint32_t ring_hi, uint32_t pend, uint32_t pm,
                                               uint32_t &span_out, uint32_t &full_out, uint32_t &first_items) {
@@ -316,6 +365,52 @@ __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint3
     c_hi = (nb + 32u + lane < lim) ? c_hi : 0u;
     uint32_t span = a.span_fixed ? a.span_fixed : 1u;
     uint32_t full = a.no_heavy;
+    const bool want_feat = (a.flags & GBS_F_FEATURES) && a.feat;
+    if (a.ctrl == kCtrlLearned || want_feat) {
+        uint32_t incl = c_lo;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        uint32_t hi_sum = c_hi;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) hi_sum += __shfl_xor_sync(FULL, hi_sum, o);
+        auto first = [&](uint32_t k) {   // entries of base buckets [nb, nb + k), k <= 32
+            return (float)__shfl_sync(FULL, incl, k - 1u);
+        };
+        const uint32_t st_b = ld_relaxed(&ctl->st_buckets), st_p = ld_relaxed(&ctl->st_phases);
+        float f[kFeat];
+        f[0] = __log2f(1.f + first(1));
+        f[1] = __log2f(1.f + first(2));
+        f[2] = __log2f(1.f + first(4));
+        f[3] = __log2f(1.f + first(8));
+        f[4] = __log2f(1.f + first(16));
+        f[5] = __log2f(1.f + first(32));
+        f[6] = __log2f(1.f + first(32) + (float)hi_sum);
+        f[7] = __log2f(1.f + (float)pend);
+        f[8] = __log2f(1.f + (float)nb);
+        f[9] = __log2f(1.f + (float)st_b);
+        f[10] = __log2f(1.f + (float)st_p);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) f[11 + i] = a.gfeat[i];
+        if (want_feat && lane == 0) {
+            const uint32_t fi = ctl->feat_n;
+            if (fi < a.feat_cap) {
+#pragma unroll
+                for (int i = 0; i < kFeat; ++i) a.feat[(size_t)fi * kFeat + i] = f[i];
+            }
+            ctl->feat_n = fi + 1u;
+        }
+        if (a.ctrl == kCtrlLearned) {
+            float y0, y1;
+            mlp_eval(a.mlp, f, y0, y1);
+            int e = (int)rintf(y0 + a.span_bias);
+            e = e < 0 ? 0 : (e > (int)kMaxSpanLog ? (int)kMaxSpanLog : e);
+            span = 1u << e;
+            full = (a.no_heavy || y1 <= 0.f) ? 1u : 0u;   // y1: logit of "split at the light bound"
+        }
+    }
     // a bucket never reaches past the smallest pending bucket
     while (span > 1u && pend > 0u && nb + span > pm) span >>= 1;
     span_out = span;
@@ -445,10 +540,15 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         next = inst < a.inst_count ? kPhInit : kPhDone;
         if (next == kPhDone) inst = kNoInst;
     }
-    // whole-run limit: a run that has not finished within run_ns is stopped
-    if (globaltimer() - U.t0 > a.run_ns) {
+    // whole-run limit: a run that has not finished within run_ns is stopped;
+    // a learned schedule also stops at its guard (the host reruns plain)
+    const unsigned long long run_t = globaltimer() - U.t0;
+    if (run_t > a.run_ns) {
         next = kPhDone;
         if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
+    } else if (a.guard_ns && run_t > a.guard_ns) {
+        next = kPhDone;
+        if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrGuard);
     }
     if (err) next = kPhDone;
     Uniform N = advance_uniform(U, next, nb);

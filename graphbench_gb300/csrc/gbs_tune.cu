@@ -15,8 +15,10 @@ using namespace gbs;
 
 namespace {
 
-// Default width multipliers and knob values explored around the best.
-const double kScales[] = {0.25, 0.5, 1.0, 2.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0, 256.0, 512.0, 1024.0, 4096.0};
+// Width multipliers 2^e of the default width: a coarse pass over kCoarse,
+// then the neighbours of the best; knob values explored around the best.
+const int kCoarse[] = {0, 3, 6, 9, 12};
+const int kMinExp = -3, kMaxExp = 14;
 const uint32_t kInline[] = {8, 16, 64, 128};
 const uint32_t kSoloEntries[] = {256, 4096, 16384};
 const uint32_t kSoloDescs[] = {16, 256, 1024};
@@ -72,34 +74,46 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
     best.delta = d0;
     double best_scale = 1.0;
     bool best_nosplit = false;
-    // 1. width for each split: walk the scales, stop two steps past a minimum
+    // 1. width for each split: coarse exponents, then the neighbours of the
+    //    best one (one and two steps on each side, twice)
     for (int split = 0; split < 2 && b.left(); ++split) {
-        double local_best = INFINITY;
-        int worse = 0;
-        for (double sc : kScales) {
-            if (!b.left() || worse >= 2) break;
-            if (split == 0 && sc == 1.0) {   // the default, timed above
-                local_best = out->default_ms;
-                continue;
-            }
-            gbs_params p = base;
-            p.delta = d0 * sc;
-            p.light = split ? INFINITY : -1.0;
+        std::vector<std::pair<int, double>> seen;   // (exponent, ms)
+        auto eval = [&](int e) -> gbs_status {
+            if (e < kMinExp || e > kMaxExp || !b.left()) return GBS_OK;
+            for (auto &q : seen)
+                if (q.first == e) return GBS_OK;
             double ms = 0.0;
-            if ((s = time_single(g, src, p, b, out->runs, ms)) != GBS_OK) return s;
-            ++out->candidates;
-            if (ms < local_best) {
-                local_best = ms;
-                worse = 0;
+            if (split == 0 && e == 0) {
+                ms = out->default_ms;   // the default, timed above
             } else {
-                ++worse;
+                gbs_params p = base;
+                p.delta = d0 * std::ldexp(1.0, e);
+                p.light = split ? INFINITY : -1.0;
+                gbs_status r = time_single(g, src, p, b, out->runs, ms);
+                if (r != GBS_OK) return r;
+                ++out->candidates;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = p;
+                    best_scale = std::ldexp(1.0, e);
+                    best_nosplit = split != 0;
+                }
             }
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = p;
-                best_scale = sc;
-                best_nosplit = split != 0;
-            }
+            seen.push_back({e, ms});
+            return GBS_OK;
+        };
+        for (int e : kCoarse)
+            if ((s = eval(e)) != GBS_OK) return s;
+        for (int round = 0; round < 2 && !seen.empty(); ++round) {
+            int be = seen[0].first;
+            double bm = seen[0].second;
+            for (auto &q : seen)
+                if (q.second < bm) {
+                    bm = q.second;
+                    be = q.first;
+                }
+            for (int d : {-1, 1, -2, 2})
+                if ((s = eval(be + d)) != GBS_OK) return s;
         }
     }
     // 2. the other knobs, one at a time around the best

@@ -81,6 +81,9 @@ typedef struct gbs_params {
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
 #define GBS_F_TRACE 0x2u     /* record one gbs_phase_rec per grid phase (gbs_trace) */
 #define GBS_F_NO_SOLO 0x4u   /* run every phase on the whole grid */
+#define GBS_F_FEATURES 0x8u  /* record the controller inputs at every bucket start (gbs_features) */
+#define GBS_F_LEARNED 0x10u  /* bucket widths from the graph's learned controller
+                                (gbs_graph_set_controller) */
 /* Failure-path test: one CTA never arrives at the first grid barrier, so every
  * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
  * wait_limit_ms and the device stays usable.  Never set in normal use. */
@@ -99,7 +102,9 @@ typedef struct gbs_stats {
     double delta_used;       /* bucket width actually used */
     double light_used;       /* light/heavy split actually used */
     uint32_t solo_phases;    /* phases run by one CTA without a grid barrier */
-    uint32_t reserved;
+    uint32_t learned;        /* bit 0: the learned controller chose the widths;
+                                bit 1: it ran past its guard and the plain schedule
+                                was run instead (the result is the plain run's) */
 } gbs_stats;
 
 /* Library / device */
@@ -180,6 +185,60 @@ typedef struct gbs_phase_rec {
 } gbs_phase_rec;
 
 gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *count);
+
+/*
+ * Learned bucket-width controller (no counterpart in the reference).  An FP32
+ * MLP, 16 inputs -> 64 -> 64 (ReLU) -> 2 outputs, evaluated by the deciding
+ * warp at every bucket start of a GBS_F_LEARNED run: output 0 predicts
+ * log2(delta / default delta), output 1 is the logit of "split light/heavy at
+ * the predicted delta" (else every edge is light).  The run's base width is
+ * 1/8 of the width predicted for the first bucket; each bucket spans 2^k base
+ * widths (k in 0..6) as output 0 says.  Inputs: log2(1 + entries) of the
+ * first 1, 2, 4, .., 64 base buckets from the bucket start, log2(1 +
+ * pending), log2(1 + bucket index), log2(1 + buckets done), log2(1 + phases
+ * done), log2(n), log2(average degree), log2(max weight), mean / max weight,
+ * log2(base width / default delta).
+ * params: 5410 floats: input means[16], input scales[16], W1[16][64], b1[64],
+ * W2[64][64], b2[64], W3[64][2], b3[2] (row-major, inputs first).  margin
+ * (<= 0: 0.25): a learned run that runs longer than (1 + margin) times the
+ * plain schedule on this graph stops and the plain schedule runs instead (the
+ * first learned run on a graph times the plain schedule first).  The
+ * distances and predecessors never depend on the schedule.  params NULL
+ * removes the controller.  The trace records of a run carry each bucket's
+ * span (bits 8-15 of kind) and whether it relaxed whole rows (bit 16).
+ */
+gbs_status gbs_graph_set_controller(gbs_graph *g, const float *params, uint32_t count, double margin);
+
+/* Controller inputs recorded by the last GBS_F_FEATURES run: 16 floats per
+ * bucket start, in order; *count receives how many were recorded. */
+gbs_status gbs_features(gbs_graph *g, float *out, uint32_t cap, uint32_t *count);
+
+/*
+ * Controller training on the GPU (hand-written forward, backward and Adam
+ * kernels; no counterpart in the reference).  A gbs_mlp holds one parameter
+ * block (layout of gbs_graph_set_controller), its gradient, Adam moments and
+ * a data set: x (n x 16 raw inputs), t (n x 2 targets: log2 of the best
+ * width scale, 1/0 for split/no split) and optional sample weights w.  Loss:
+ * sum_i w_i [(y0 - t0)^2 + BCE(sigmoid(y1), t1)] / sum_i w_i.  The input
+ * means and scales in the block are not trained.
+ */
+typedef struct gbs_mlp gbs_mlp;
+gbs_status gbs_mlp_create(gbs_mlp **out);
+gbs_status gbs_mlp_destroy(gbs_mlp *m);
+gbs_status gbs_mlp_set_params(gbs_mlp *m, const float *params);   /* 5410 floats; resets Adam */
+gbs_status gbs_mlp_get_params(gbs_mlp *m, float *params);
+gbs_status gbs_mlp_set_data(gbs_mlp *m, const float *x, const float *t, const float *w, uint32_t n);
+/* Loss and gradient over samples [first, first + count) in stored order;
+ * grad (5378 floats: W1, b1, W2, b2, W3, b3) may be NULL. */
+gbs_status gbs_mlp_loss_grad(gbs_mlp *m, uint32_t first, uint32_t count, double *loss, float *grad);
+/* One Adam step with the last gradient. */
+gbs_status gbs_mlp_adam(gbs_mlp *m, float lr, float beta1, float beta2, float eps);
+/* Minibatch Adam (beta 0.9 / 0.999, eps 1e-8), samples reshuffled every
+ * epoch; epoch_loss (epochs entries, may be NULL) gets the mean batch loss. */
+gbs_status gbs_mlp_train(gbs_mlp *m, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                         double *epoch_loss);
+/* Outputs for n raw input rows (n x 2). */
+gbs_status gbs_mlp_predict(gbs_mlp *m, const float *x, uint32_t n, float *y);
 
 /*
  * Batched SSSP: many independent instances in one persistent launch.

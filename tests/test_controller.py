@@ -1,0 +1,169 @@
+"""The learned bucket-width controller.
+
+CPU: the oracle's analytic gradient agrees with finite differences (so it can
+judge the CUDA kernels), and the committed parameter block is well formed.
+GPU: the CUDA forward/backward kernels' loss and gradient equal the oracle's
+within FP32 tolerance; an Adam step equals the oracle's; training lowers the
+loss; learned runs are bit-identical to plain ones, the guard falls back to
+the plain schedule, and the trained controller beats the plain fixed delta on
+held-out graphs."""
+import numpy as np
+import pytest
+
+from oracle import mlp as ref
+
+# FP32 kernels against a float64 restatement, relative to the largest entry
+GRAD_RTOL = 2e-4
+
+
+def _data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(3.0, 2.0, size=(n, 16)).astype(np.float32)
+    t = np.stack([rng.normal(1.0, 2.0, n), rng.integers(0, 2, n)], axis=1).astype(np.float32)
+    w = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    return x, t, w
+
+
+def test_oracle_gradient_matches_finite_differences():
+    x, t, w = _data(40, 1)
+    p = ref.init_params(3, mu=x.mean(0), sd=x.std(0) + 1e-3).astype(np.float64)
+    _, g = ref.loss_grad(p, x, t, w)
+    rng = np.random.default_rng(0)
+    for k in rng.choice(len(g), 60, replace=False):
+        e = np.zeros_like(p)
+        e[ref.OFF_W1 + k] = 1e-6
+        num = (ref.loss_grad(p + e, x, t, w)[0] - ref.loss_grad(p - e, x, t, w)[0]) / 2e-6
+        assert abs(num - g[k]) <= 1e-6 + 1e-4 * abs(g[k]), (k, num, g[k])
+
+
+def test_committed_controller_block(gb):
+    from graphbench_gb300 import controller
+    p = controller.load()
+    assert p.shape == (gb.MLP_FLOATS,) and p.dtype == np.float32
+    assert np.all(np.isfinite(p)) and np.all(p[16:32] > 0)
+
+
+@pytest.mark.gpu
+def test_cuda_loss_and_gradient_match_oracle(gb):
+    x, t, w = _data(1000, 2)
+    p = ref.init_params(5, mu=x.mean(0), sd=x.std(0) + 1e-3)
+    m = gb.Mlp(p)
+    m.set_data(x, t, w)
+    for first, count in [(0, 1000), (17, 300), (999, 1)]:
+        loss, g = m.loss_grad(first, count)
+        rl, rg = ref.loss_grad(p, x[first:first + count], t[first:first + count], w[first:first + count])
+        assert abs(loss - rl) <= 1e-5 * max(1.0, abs(rl))
+        assert np.max(np.abs(g - rg)) <= GRAD_RTOL * np.max(np.abs(rg)), (first, count)
+    y = m.predict(x[:50])
+    ry, _ = ref.forward(p, x[:50])
+    assert np.max(np.abs(y - ry)) <= 1e-4 * max(1.0, np.max(np.abs(ry)))
+    m.close()
+
+
+@pytest.mark.gpu
+def test_cuda_adam_step_matches_oracle(gb):
+    x, t, w = _data(256, 4)
+    p = ref.init_params(7, mu=x.mean(0), sd=x.std(0) + 1e-3)
+    m = gb.Mlp(p)
+    m.set_data(x, t, w)
+    mom = np.zeros(gb.MLP_PARAMS)
+    vel = np.zeros(gb.MLP_PARAMS)
+    rp = p.astype(np.float64)
+    for step in range(1, 4):
+        m.loss_grad()
+        m.adam(1e-2)
+        _, rg = ref.loss_grad(rp, x, t, w)
+        rp, mom, vel = ref.adam(rp, rg, mom, vel, step, 1e-2)
+    got = m.params().astype(np.float64)
+    assert np.max(np.abs(got - rp)) <= 1e-4 * max(1.0, np.max(np.abs(rp)))
+    m.close()
+
+
+@pytest.mark.gpu
+def test_cuda_training_lowers_loss(gb):
+    rng = np.random.default_rng(9)
+    x = rng.normal(0, 1, size=(4096, 16)).astype(np.float32)
+    t = np.stack([x[:, 0] * 2 - x[:, 3], (x[:, 5] > 0)], axis=1).astype(np.float32)
+    m = gb.Mlp(ref.init_params(1))
+    m.set_data(x, t)
+    losses = m.train(epochs=30, batch=256, lr=3e-3, seed=1)
+    assert losses[-1] < 0.2 * losses[0], losses[[0, -1]]
+    m.close()
+
+
+def _learned_graph(gb, host):
+    from graphbench_gb300 import controller
+    g = gb.Graph.from_host(host)
+    g.set_controller(controller.load())
+    return g
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["rmat", "grid"])
+def test_learned_runs_bit_identical_to_plain(kind, gb, orc):
+    host = gb.gen_rmat(13, 16, 31) if kind == "rmat" else gb.gen_grid(128, 160, 8, "f32")
+    srcs = gb.sample_sources(host, 4, 3) if kind == "rmat" else [0, 77]
+    with _learned_graph(gb, host) as g:
+        for s in srcs:
+            d, p, st = g.sssp(int(s), flags=gb.F_LEARNED | gb.F_TRACE)
+            assert st["learned"] & 1
+            tr = g.trace()
+            assert all(1 <= r["span"] <= 64 for r in tr)
+            d0, p0, _ = g.sssp(int(s))
+            assert np.array_equal(d, d0) and np.array_equal(p, p0)
+            assert np.array_equal(d, orc.dijkstra(host.row, host.col, host.w, int(s)))
+
+
+@pytest.mark.gpu
+def test_feature_recording(gb):
+    a = gb.gen_rmat(11, 16, 4)
+    with gb.Graph.from_host(a) as g:
+        _, _, st = g.sssp(0, flags=gb.F_FEATURES)
+        f = g.features()
+    # one row per bucket start after bucket 0, whose width the host picks
+    assert len(f) == st["buckets"] - 1 and f.shape[1] == gb.N_FEAT
+    assert np.all(np.isfinite(f))
+    assert np.all(np.diff(f[:, 8]) > 0)             # log2(1 + bucket index) grows
+    assert np.allclose(f[:, 11], np.log2(a.n))
+
+
+@pytest.mark.gpu
+def test_learned_guard_falls_back_to_plain(gb, orc):
+    """A controller that always asks for a width 2^-20 of the plain one makes
+    millions of buckets: the learned run passes its guard ((1 + margin) x the
+    plain time), stops, and the plain schedule gives the result."""
+    from graphbench_gb300 import controller
+    host = gb.gen_grid(96, 96, 2, "f32")
+    p = controller.load().copy()
+    p[ref.OFF_W3:ref.OFF_B3] = 0.0
+    p[ref.OFF_B3] = -30.0      # y0: log2(width / plain width)
+    with gb.Graph.from_host(host) as g:
+        g.set_controller(p, margin=0.5)
+        d, pr, st = g.sssp(0, flags=gb.F_LEARNED)   # first: times the plain schedule
+        assert st["learned"] == 3
+        d2, _, st2 = g.sssp(0, flags=gb.F_LEARNED)
+        assert st2["learned"] == 3
+    ref_d = orc.dijkstra(host.row, host.col, host.w, 0)
+    assert np.array_equal(d, ref_d) and np.array_equal(d2, ref_d)
+    assert np.array_equal(pr, orc.min_tight_pred(host.row, host.col, host.w, 0, ref_d))
+
+
+@pytest.mark.gpu
+def test_trained_controller_beats_plain_on_held_out_graphs(gb):
+    """The committed controller on graphs and seeds outside its training set:
+    total kernel time of learned runs below the plain fixed delta's (a run
+    that fell back to plain is charged twice its time)."""
+    cases = [(gb.gen_grid(768, 768, 97, "f32"), [0]), (gb.gen_rmat(18, 16, 77), None)]
+    for host, srcs in cases:
+        srcs = srcs if srcs is not None else [int(s) for s in gb.sample_sources(host, 6, 5)]
+        with _learned_graph(gb, host) as g:
+            g.sssp(srcs[0], flags=gb.F_LEARNED)   # plain timing + warm-up
+            g.sssp(srcs[0])
+            plain = learned = 0.0
+            for s in srcs:
+                for _ in range(2):
+                    _, _, a = g.sssp(s, want_dist=False, want_pred=False)
+                    _, _, b = g.sssp(s, want_dist=False, want_pred=False, flags=gb.F_LEARNED)
+                    plain += a["kernel_ms"]
+                    learned += b["kernel_ms"] if b["learned"] == 1 else b["kernel_ms"] * 2
+            assert learned < plain, (host.n, learned, plain)
