@@ -14,6 +14,16 @@ persistent launch).  Inputs are synthetic (seeded generator in the library).
   e2e    = same metric through gbs_sssp with pinned HOST output buffers
            (device->host copy of dist + pred inside the timed call)
 
+Beside the plain kernel, on the same resident graph and the same sources:
+  learned    every step with the learned bucket-width controller (the
+             committed block, flags=F_LEARNED; a run past its guard reruns
+             plain and is charged both runs)
+  autotuned  every step with the schedule gbs_autotune picked on 4 sources
+  batched    all sources in one persistent launch replayed from a CUDA graph
+             (gbs_plan_sources with the parameters gbs_autotune_plan_sources
+             picked), dist/pred of every source kept on the device
+Each reports GTEPS and its ratio to the plain value.
+
 Multi-GPU: one process per GPU (torchrun); every rank runs the whole workload
 on its own GPU (replicas: a single SSSP does not shard); value = sum over
 ranks / max time.  ``--impl reference`` times the reference's own CPU code.
@@ -193,6 +203,58 @@ def cpu_baseline_port(g, srcs, delta, budget_s: float):
                       f"run_sspath_arr (serial), {t_total:.1f} s"}
 
 
+def arm_learned(gb, g, order, W, K):
+    from graphbench_gb300 import controller
+    g.set_controller(controller.load())
+    for i in range(W):
+        g.sssp_device(order[i], flags=gb.F_LEARNED)
+    ms = edges = 0.0
+    reverted = 0
+    for i in range(W, W + K):
+        st = g.sssp_device(order[i], flags=gb.F_LEARNED)
+        ms += st["device_ms"]
+        edges += st["edges_reached"]
+        reverted += 1 if st["learned"] == 3 else 0
+    g.set_controller(None)
+    return {"value": edges / ms / 1e6, "unit": "GTEPS", "ms_per_step": ms / K, "steps": K,
+            "reverted_to_plain": reverted,
+            "path": "gbs_sssp_device, flags=GBS_F_LEARNED, committed controller block"}
+
+
+def arm_autotuned(gb, g, order, W, K, srcs):
+    t0 = time.time()
+    kw, rep = g.autotune([int(s) for s in srcs[:4]], budget_ms=3000)
+    tune_s = time.time() - t0
+    for i in range(W):
+        g.sssp_device(order[i], **kw)
+    ms = edges = 0.0
+    for i in range(W, W + K):
+        st = g.sssp_device(order[i], **kw)
+        ms += st["device_ms"]
+        edges += st["edges_reached"]
+    return {"value": edges / ms / 1e6, "unit": "GTEPS", "ms_per_step": ms / K, "steps": K,
+            "schedule": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in kw.items()},
+            "delta_scale": rep["delta_scale"], "no_split": rep["no_split"], "tune_seconds": round(tune_s, 1)}
+
+
+def arm_batched(gb, g, srcs, reps: int = 5):
+    t0 = time.time()
+    bp, rep = gb.autotune_plan(g, srcs, budget_ms=4000)
+    tune_s = time.time() - t0
+    with gb.Plan(g, srcs, params=bp) as plan:
+        for _ in range(2):
+            plan.run()
+        ms = edges = 0.0
+        for _ in range(reps):
+            st = plan.run()
+            ms += st["device_ms"]
+            edges += st["edges_reached"]
+    return {"value": edges / ms / 1e6, "unit": "GTEPS", "ms_per_launch": ms / reps, "instances": len(srcs),
+            "launches": reps, "group_ctas": st["group_ctas"], "groups": st["groups"],
+            "params": dict(rep["best"]), "tune_seconds": round(tune_s, 1),
+            "path": "gbs_plan_sources + gbs_plan_launch (CUDA graph), outputs on the device"}
+
+
 # ----------------------------------------------------------------- our arm
 def run_ours(args):
     world, rank, local = dist_env()
@@ -272,7 +334,8 @@ def run_ours(args):
                    avg_device_ms=dev_s * 1e3 / K,
                    wall_ms_per_step=wall * 1e3 / K)
         result = {
-            "metric": "GTEPS SSSP (plain fixed-delta delta-stepping)",
+            "metric": "GTEPS SSSP, learned/batched vs plain fixed-delta on 1 GB300; % HBM roofline",
+            "value_is": "plain fixed-delta delta-stepping (learned / autotuned / batched: see those keys)",
             "value": edges_all / dev_max / 1e9,
             "unit": "GTEPS",
             "n_gpus": world,
@@ -302,6 +365,18 @@ def run_ours(args):
             "clocks": clocks,
             "wall_ms_per_step": wall_max * 1e3 / K,
         }
+        if world == 1 and not args.no_arms:
+            plain = result["value"]
+            for name, fn in (("learned", lambda: arm_learned(gb, g, order, W, K)),
+                             ("autotuned", lambda: arm_autotuned(gb, g, order, W, K, srcs)),
+                             ("batched", lambda: arm_batched(gb, g, srcs))):
+                try:
+                    arm = fn()
+                    arm["vs_plain"] = arm["value"] / plain
+                except Exception as e:  # pragma: no cover
+                    arm = {"value": None, "error": str(e)}
+                result[name] = arm
+                log(f"[rank 0] {name}: {arm.get('value')}")
         if world == 1 and not args.no_cpu_baseline:
             try:
                 result["cpu_baseline"] = cpu_baseline_port(hg, srcs, st0["delta_used"], args.cpu_budget_s)
@@ -390,7 +465,8 @@ def run_reference(args):
               f"edge factor, weights, delta rule and source seed as {args.workload}); stand-in size because "
               f"one scale-{wl.get('scale')} run takes minutes on one core")
     print(json.dumps({
-        "impl": "reference", "metric": "GTEPS SSSP (plain fixed-delta delta-stepping)", "value": val,
+        "impl": "reference", "metric": "GTEPS SSSP, learned/batched vs plain fixed-delta on 1 GB300; % HBM roofline",
+        "value_is": "the reference's serial run_sspath_arr, plain fixed delta", "value": val,
         "unit": "GTEPS", "n_gpus": world, "steps": done, "warmup": min(W, 1), "ms_per_step": secs * 1e3 / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference doubles)",
         "data": "synthetic", "config": {"workload": f"{args.workload}_{wl['wtype']}", "reference_scale": scale,
@@ -411,6 +487,7 @@ def main():
     ap.add_argument("--light", type=float, default=None)
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-arms", action="store_true", help="skip the learned / autotuned / batched arms")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-scale", type=int, default=16)
     ap.add_argument("--ref-procs", type=int, default=16)
