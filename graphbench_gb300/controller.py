@@ -13,6 +13,10 @@ and Adam kernels (``Mlp``), on traces of the plain method:
    every bucket start (``GBS_F_FEATURES``);
 3. every recorded input is labelled with the graph's best (log2 width
    scale, split); samples are weighted so that each graph counts once.
+   Every width at or above the largest distance gives the same schedule (one
+   bucket), so the label is capped at the first such width: otherwise small
+   graphs, where every width past that point ties, give labels spread over
+   the whole flat end of the sweep.
 
 Distances never depend on the width, so the controller can only change the
 run time; the library checks that by falling back to the plain schedule when
@@ -88,6 +92,12 @@ def collect_graph(spec: dict, tune_budget_ms: float = 800.0, feature_scales=(1 /
         best = float(rep["delta_scale"])
         split = 0.0 if rep["no_split"] else 1.0
         d0 = g.info()["default_delta"]
+        d, _, _ = g.sssp(srcs[0], want_pred=False)
+        unreached = np.float32(np.inf) if d.dtype == np.float32 else np.uint32(0xFFFFFFFF)
+        fin = d[d != unreached].astype(np.float64)
+        maxdist = float(fin.max()) if len(fin) else d0
+        one_bucket = 2.0 ** math.ceil(math.log2(max(maxdist / d0, 1.0)))
+        best = min(best, one_bucket)
         rows = []
         for f in sorted(set([*feature_scales, 1.0 / best])):
             light = None if split else math.inf

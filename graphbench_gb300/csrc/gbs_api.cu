@@ -335,10 +335,11 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     float span_bias = 0.f;
     uint32_t span0 = 1, full0 = 0;
     if (learned) {
-        // the controller's first prediction (bucket 0 holds only the source)
-        // fixes the base width: 1/8 of the predicted delta, so spans of 1..64
-        // base widths reach 8x below and 8x above it; the split is at the
-        // predicted delta
+        // the controller's first prediction (bucket 0 holds only the source),
+        // clamped to the range the training labels cover, fixes the base
+        // width: half the predicted delta, so spans of 1..64 base widths reach
+        // 2x below and 32x above it and the ring window holds 32 predicted
+        // widths; the split is at the predicted delta
         float x[kFeat];
         for (int i = 0; i < 7; ++i) x[i] = 1.f;
         for (int i = 7; i < 11; ++i) x[i] = 0.f;
@@ -346,8 +347,8 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
         x[15] = 0.f;
         float y1 = 0.f;
         const float y0 = mlp_host(g->mlp_host.data(), x, y1);
-        const double p0 = std::rint(std::min(std::max((double)y0, -20.0), 30.0));
-        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 3.0), d_def * std::exp2(p0));
+        const double p0 = std::rint(std::min(std::max((double)y0, -2.0), 14.0));
+        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 1.0), d_def * std::exp2(p0));
         span_bias = (float)std::log2(d_def / r.delta);
         int e0 = (int)std::rint(y0 + span_bias);
         e0 = std::min(std::max(e0, 0), (int)kMaxSpanLog);

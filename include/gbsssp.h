@@ -192,8 +192,9 @@ gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *c
  * warp at every bucket start of a GBS_F_LEARNED run: output 0 predicts
  * log2(delta / default delta), output 1 is the logit of "split light/heavy at
  * the predicted delta" (else every edge is light).  The run's base width is
- * 1/8 of the width predicted for the first bucket; each bucket spans 2^k base
- * widths (k in 0..6) as output 0 says.  Inputs: log2(1 + entries) of the
+ * half the width predicted for the first bucket (that prediction clamped to
+ * 2^-2 .. 2^14 times the default); each bucket spans 2^k base widths (k in
+ * 0..6) as output 0 says.  Inputs: log2(1 + entries) of the
  * first 1, 2, 4, .., 64 base buckets from the bucket start, log2(1 +
  * pending), log2(1 + bucket index), log2(1 + buckets done), log2(1 + phases
  * done), log2(n), log2(average degree), log2(max weight), mean / max weight,

@@ -129,16 +129,17 @@ def test_feature_recording(gb):
 
 @pytest.mark.gpu
 def test_learned_guard_falls_back_to_plain(gb, orc):
-    """A controller that always asks for a width 2^-20 of the plain one makes
-    millions of buckets: the learned run passes its guard ((1 + margin) x the
-    plain time), stops, and the plain schedule gives the result."""
+    """A controller that always asks for the finest width it may (1/8 of the
+    plain one) on a grid, where wide buckets pay: the learned run passes its
+    guard ((1 + margin) x the plain time), stops, and the plain schedule gives
+    the result."""
     from graphbench_gb300 import controller
     host = gb.gen_grid(96, 96, 2, "f32")
     p = controller.load().copy()
     p[ref.OFF_W3:ref.OFF_B3] = 0.0
     p[ref.OFF_B3] = -30.0      # y0: log2(width / plain width)
     with gb.Graph.from_host(host) as g:
-        g.set_controller(p, margin=0.5)
+        g.set_controller(p, margin=1e-6)
         d, pr, st = g.sssp(0, flags=gb.F_LEARNED)   # first: times the plain schedule
         assert st["learned"] == 3
         d2, _, st2 = g.sssp(0, flags=gb.F_LEARNED)
