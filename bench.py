@@ -17,7 +17,8 @@ persistent launch).  Inputs are synthetic (seeded generator in the library).
 Beside the plain kernel, on the same resident graph and the same sources:
   learned    every step with the learned bucket-width controller (the
              committed block, flags=F_LEARNED; a run past its guard reruns
-             plain and is charged both runs)
+             plain and the step is charged both runs; after that the graph
+             runs plain)
   autotuned  every step with the schedule gbs_autotune picked on 4 sources
   batched    all sources in one persistent launch replayed from a CUDA graph
              (gbs_plan_sources with the parameters gbs_autotune_plan_sources
@@ -209,15 +210,15 @@ def arm_learned(gb, g, order, W, K):
     for i in range(W):
         g.sssp_device(order[i], flags=gb.F_LEARNED)
     ms = edges = 0.0
-    reverted = 0
+    counts = {1: 0, 2: 0, 3: 0}
     for i in range(W, W + K):
         st = g.sssp_device(order[i], flags=gb.F_LEARNED)
-        ms += st["device_ms"]
+        ms += st["device_ms"]          # includes any abandoned learned run
         edges += st["edges_reached"]
-        reverted += 1 if st["learned"] == 3 else 0
+        counts[st["learned"]] = counts.get(st["learned"], 0) + 1
     g.set_controller(None)
     return {"value": edges / ms / 1e6, "unit": "GTEPS", "ms_per_step": ms / K, "steps": K,
-            "reverted_to_plain": reverted,
+            "learned_steps": counts[1], "fell_back_steps": counts[3], "plain_after_loss_steps": counts[2],
             "path": "gbs_sssp_device, flags=GBS_F_LEARNED, committed controller block"}
 
 

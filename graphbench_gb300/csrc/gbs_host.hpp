@@ -56,6 +56,7 @@ struct gbs_graph {
     std::vector<float> mlp_host;
     double ctrl_margin = 0.25;
     double plain_ms = 0.0;        // kernel time of the plain schedule on this graph (the guard)
+    bool ctrl_lost = false;       // a learned run lost to plain here: run plain from now on
     // recorded controller inputs (GBS_F_FEATURES)
     float *d_feat = nullptr;
     uint32_t feat_cap = 0, feat_n = 0;

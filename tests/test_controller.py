@@ -143,7 +143,8 @@ def test_learned_guard_falls_back_to_plain(gb, orc):
         d, pr, st = g.sssp(0, flags=gb.F_LEARNED)   # first: times the plain schedule
         assert st["learned"] == 3
         d2, _, st2 = g.sssp(0, flags=gb.F_LEARNED)
-        assert st2["learned"] == 3
+        assert st2["learned"] == 2                  # lost here before: plain directly
+        assert st["kernel_ms"] > st2["kernel_ms"]    # the first call paid for three runs
     ref_d = orc.dijkstra(host.row, host.col, host.w, 0)
     assert np.array_equal(d, ref_d) and np.array_equal(d2, ref_d)
     assert np.array_equal(pr, orc.min_tight_pred(host.row, host.col, host.w, 0, ref_d))
@@ -152,8 +153,8 @@ def test_learned_guard_falls_back_to_plain(gb, orc):
 @pytest.mark.gpu
 def test_trained_controller_beats_plain_on_held_out_graphs(gb):
     """The committed controller on graphs and seeds outside its training set:
-    total kernel time of learned runs below the plain fixed delta's (a run
-    that fell back to plain is charged twice its time)."""
+    total kernel time of learned runs below the plain fixed delta's (a call
+    whose learned run fell back is charged both runs)."""
     cases = [(gb.gen_grid(768, 768, 97, "f32"), [0]), (gb.gen_rmat(18, 16, 77), None)]
     for host, srcs in cases:
         srcs = srcs if srcs is not None else [int(s) for s in gb.sample_sources(host, 6, 5)]
@@ -166,5 +167,5 @@ def test_trained_controller_beats_plain_on_held_out_graphs(gb):
                     _, _, a = g.sssp(s, want_dist=False, want_pred=False)
                     _, _, b = g.sssp(s, want_dist=False, want_pred=False, flags=gb.F_LEARNED)
                     plain += a["kernel_ms"]
-                    learned += b["kernel_ms"] if b["learned"] == 1 else b["kernel_ms"] * 2
+                    learned += b["kernel_ms"]   # includes any abandoned run
             assert learned < plain, (host.n, learned, plain)
