@@ -28,7 +28,7 @@ STATUS = {
     0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "NO_MEMORY", 4: "CAPACITY",
     5: "TIMEOUT", 6: "OVERFLOW", 7: "UNSUPPORTED", 8: "INTERNAL",
 }
-W_U32, W_F32 = 0, 1
+W_U32, W_F32, W_F64 = 0, 1, 2
 F_NO_STATS = 0x1
 
 # Every symbol include/gbsssp.h declares (tests check the library exports them).
@@ -343,11 +343,13 @@ class Graph:
             self.wtype = W_F32
         elif w.dtype == np.uint32:
             self.wtype = W_U32
+        elif w.dtype == np.float64:
+            self.wtype = W_F64
         else:
-            raise TypeError("weights must be uint32 or float32")
+            raise TypeError("weights must be uint32, float32 or float64")
         self.n = len(row) - 1
         self.m = int(row[-1]) if len(row) else 0
-        self.dist_dtype = np.float32 if self.wtype == W_F32 else np.uint32
+        self.dist_dtype = {W_F32: np.float32, W_U32: np.uint32, W_F64: np.float64}[self.wtype]
         h = ctypes.c_void_p()
         _check(lib.gbs_graph_create(self.n, len(col), _ptr(row), _ptr(col), _ptr(w), self.wtype,
                                     ctypes.byref(h)), "gbs_graph_create")
@@ -508,18 +510,15 @@ def _tcsr_to_graph(gs: TCsr) -> Graph:
     w = np.asarray(gs.edge_weight, dtype=np.float64)
     if np.all(w == np.floor(w)) and (len(w) == 0 or (w.min() >= 0 and w.max() < 2**32 - 1)):
         return Graph(row, gs.edge_idx, w.astype(np.uint32))
-    w32 = w.astype(np.float32)
-    if not np.array_equal(w32.astype(np.float64), w):
-        raise GbsError(7, "run_sspath_arr", "fractional double weights that are not exactly float32")
-    return Graph(row, gs.edge_idx, w32)
+    return Graph(row, gs.edge_idx, w)
 
 
 def run_sspath_arr(gs: TCsr, source: int, delta: float) -> np.ndarray:
     """Mirror of run_sspath_arr(gs, predecesor, source, delta)
     (sssp/csr_sspath_array.c:149): fills gs.weight with float64 distances
     (inf for unreached) and returns them.  Integer weights run on the uint32
-    path (exact in double); float32-representable weights on the float32
-    path."""
+    path (exact in double); other weights on the float64 path, the
+    reference's own arithmetic."""
     with _tcsr_to_graph(gs) as g:
         dist, _, _ = g.sssp(int(source), delta=float(delta), want_pred=False)
     out = dist.astype(np.float64)

@@ -45,10 +45,13 @@ __global__ void k_mid(const uint32_t *__restrict__ row, const uint2 *__restrict_
     }
 }
 
+// src_word: the source's state word (uint32 / float32: dist 0, pred = src;
+// float64: the distance 0.0 alone)
 __global__ void k_reset(unsigned long long *__restrict__ dp, uint32_t *__restrict__ tag, uint32_t n,
-                        uint32_t src, uint32_t *__restrict__ ring0, Ctl *ctl, uint32_t span0, uint32_t full0) {
+                        uint32_t src, unsigned long long src_word, uint32_t *__restrict__ ring0, Ctl *ctl,
+                        uint32_t span0, uint32_t full0) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        dp[v] = (v == src) ? (unsigned long long)src : kUnreached;   // dist 0, pred = src
+        dp[v] = (v == src) ? src_word : kUnreached;
         tag[v] = (v == src) ? 0u : kTagInit;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -71,6 +74,55 @@ __global__ void k_unpack(const unsigned long long *__restrict__ dp, uint32_t n, 
         const bool reached = x != kUnreached;
         if (dist) dist[v] = reached ? (uint32_t)(x >> 32) : (F32 ? 0x7F800000u : 0xFFFFFFFFu);
         if (pred) pred[v] = reached ? (v == src ? (int32_t)src : (int32_t)(uint32_t)x) : -1;
+    }
+}
+
+// float64 runs: dp holds the distance alone.  dist gets the double (+inf
+// unreached); pred starts at the source / "not found yet" / -1 for k_pred64.
+constexpr unsigned long long kInfBits64 = 0x7FF0000000000000ull;
+__global__ void k_unpack64(const unsigned long long *__restrict__ dp, uint32_t n, uint32_t src,
+                           unsigned long long *__restrict__ dist, int32_t *__restrict__ pred) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const unsigned long long x = dp[v];
+        const bool reached = x != kUnreached;
+        if (dist) dist[v] = reached ? x : kInfBits64;
+        if (pred) pred[v] = reached ? (v == src ? (int32_t)src : INT32_MAX) : -1;
+    }
+}
+
+// float64 predecessors: the smallest u with an edge (u, v) and dist[u] + w ==
+// dist[v] in double (the same rounded add as the relaxation).  One warp per
+// row; every reached vertex other than the source has such an edge.
+__global__ void k_pred64(const uint32_t *__restrict__ row, const uint2 *__restrict__ adj,
+                         const unsigned long long *__restrict__ w64, const unsigned long long *__restrict__ dp,
+                         uint32_t n, uint32_t src, int32_t *__restrict__ pred) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+        const unsigned long long du = dp[u];
+        if (du == kUnreached) continue;
+        const double d = __longlong_as_double((long long)du);
+        for (uint32_t e = row[u] + lane; e < row[u + 1]; e += 32u) {
+            const uint32_t v = adj[e].x;
+            if (v == src) continue;
+            const unsigned long long dv = __ldg(dp + v);
+            if (dv == kUnreached) continue;
+            const double s = __dadd_rn(d, __longlong_as_double((long long)w64[e]));
+            if ((unsigned long long)__double_as_longlong(s) == dv) atomicMin(pred + v, (int32_t)u);
+        }
+    }
+}
+
+__global__ void k_mid64(const uint32_t *__restrict__ row, const unsigned long long *__restrict__ w64, uint32_t n,
+                        unsigned long long light_bits, uint32_t *__restrict__ mid) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t lo = row[v], hi = row[v + 1];
+        while (lo < hi) {  // first edge with weight > light
+            const uint32_t m = lo + ((hi - lo) >> 1);
+            if (w64[m] <= light_bits) lo = m + 1;
+            else hi = m;
+        }
+        mid[v] = lo;
     }
 }
 
@@ -124,21 +176,70 @@ void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits,
     for (auto &t : th) t.join();
 }
 
+// float64 rows: sorted by (weight bits, col); adj gets {col, 0}, w64 the
+// weights in the same order.
+void sort_rows64(const uint64_t *row, const uint32_t *cols, const uint64_t *wbits, uint32_t n,
+                 std::vector<uint2> &adj, std::vector<unsigned long long> &w64) {
+    unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::atomic<uint32_t> next{0};
+    const uint32_t grain = 4096;
+    auto worker = [&]() {
+        std::vector<std::pair<uint64_t, uint32_t>> keys;
+        for (;;) {
+            const uint32_t v0 = next.fetch_add(grain);
+            if (v0 >= n) break;
+            const uint32_t v1 = std::min<uint64_t>((uint64_t)v0 + grain, n);
+            for (uint32_t v = v0; v < v1; ++v) {
+                const uint64_t b = row[v], e = row[v + 1];
+                keys.resize(e - b);
+                for (uint64_t i = b; i < e; ++i) keys[i - b] = {wbits[i], cols[i]};
+                std::sort(keys.begin(), keys.end());
+                for (uint64_t i = b; i < e; ++i) {
+                    adj[i] = make_uint2(keys[i - b].second, 0u);
+                    w64[i] = keys[i - b].first;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; ++t) th.emplace_back(worker);
+    worker();
+    for (auto &t : th) t.join();
+}
+
 gbs_status prepare_csr(uint32_t n, uint64_t m, const uint64_t *row_offsets, const uint32_t *cols,
                        const void *weights, gbs_weight_type wtype, std::vector<uint32_t> &row32,
-                       std::vector<uint2> &adj, double &max_w) {
+                       std::vector<uint2> &adj, double &max_w, std::vector<unsigned long long> *w64) {
     if (!row_offsets || (m && (!cols || !weights)))
         return fail(GBS_ERR_INVALID_ARG, "NULL CSR array");
-    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32)
-        return fail(GBS_ERR_INVALID_ARG, "unknown weight type");
+    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32 && !(wtype == GBS_WEIGHT_F64 && w64))
+        return fail(GBS_ERR_INVALID_ARG, "unknown or unsupported weight type");
     if (n == 0 || n > 0x7FFFFFFFu) return fail(GBS_ERR_INVALID_ARG, "vertex count must be in [1, 2^31)");
     if (m >= 0xFFFFFFFFull) return fail(GBS_ERR_UNSUPPORTED, "edge count must be < 2^32");
     if (row_offsets[0] != 0 || row_offsets[n] != m)
         return fail(GBS_ERR_INVALID_ARG, "row_offsets must start at 0 and end at m");
     for (uint32_t v = 0; v < n; ++v)
         if (row_offsets[v + 1] < row_offsets[v]) return fail(GBS_ERR_INVALID_ARG, "row_offsets decrease");
-    std::vector<uint32_t> wbits(m);
     max_w = 0.0;
+    if (wtype == GBS_WEIGHT_F64) {
+        std::vector<uint64_t> wb(m);
+        for (uint64_t e = 0; e < m; ++e) {
+            if (cols[e] >= n) return fail(GBS_ERR_INVALID_ARG, "column index out of range");
+            double w = ((const double *)weights)[e];
+            if (!(w >= 0.0) || std::isinf(w))
+                return fail(GBS_ERR_INVALID_ARG, "float64 weights must be finite and >= 0");
+            if (w == 0.0) w = 0.0;  // -0.0 -> +0.0
+            std::memcpy(&wb[e], &w, 8);
+            if (w > max_w) max_w = w;
+        }
+        adj.resize(m);
+        w64->resize(m);
+        sort_rows64(row_offsets, cols, wb.data(), n, adj, *w64);
+        row32.resize((size_t)n + 1);
+        for (uint32_t v = 0; v <= n; ++v) row32[v] = (uint32_t)row_offsets[v];
+        return GBS_OK;
+    }
+    std::vector<uint32_t> wbits(m);
     for (uint64_t e = 0; e < m; ++e) {
         if (cols[e] >= n) return fail(GBS_ERR_INVALID_ARG, "column index out of range");
         if (wtype == GBS_WEIGHT_U32) {
@@ -190,9 +291,16 @@ void free_workspace(Workspace &w) {
     w = Workspace{};
 }
 
-int persistent_ctas_per_sm(bool f32, bool batch) {
-    const void *kfn = batch ? (f32 ? (const void *)sssp_batch<true> : (const void *)sssp_batch<false>)
-                            : (f32 ? (const void *)sssp_persistent<true> : (const void *)sssp_persistent<false>);
+int persistent_ctas_per_sm(gbs_weight_type wt, bool batch) {
+    const void *kfn;
+    if (batch) {
+        if (wt == GBS_WEIGHT_F64) return 0;   // batched launches take uint32 / float32 graphs
+        kfn = wt == GBS_WEIGHT_F32 ? (const void *)sssp_batch<kWF32> : (const void *)sssp_batch<kWU32>;
+    } else {
+        kfn = wt == GBS_WEIGHT_F64   ? (const void *)sssp_persistent<kWF64>
+              : wt == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<kWF32>
+                                     : (const void *)sssp_persistent<kWU32>;
+    }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kTPB, 0) != cudaSuccess) {
         cudaGetLastError();
@@ -218,11 +326,11 @@ gbs_status ensure_workspace(gbs_graph *g) {
     GBS_CUDA(cudaMalloc(&g->ws.mid, sizeof(uint32_t) * n));
     g->ws.trace = nullptr;
     g->ws.trace_cap = 0;
-    GBS_CUDA(cudaMalloc(&g->d_dist, sizeof(uint32_t) * n));
+    GBS_CUDA(cudaMalloc(&g->d_dist, dist_bytes(g->wtype) * n));
     GBS_CUDA(cudaMalloc(&g->d_pred, sizeof(int32_t) * n));
     g->epoch = 1;
     g->hround = 1;
-    const int per_sm = persistent_ctas_per_sm(g->wtype == GBS_WEIGHT_F32, false);
+    const int per_sm = persistent_ctas_per_sm(g->wtype, false);
     if (per_sm < 1) return fail(GBS_ERR_UNSUPPORTED, "persistent kernel cannot be resident");
     g->blocks = per_sm * g->sms;
     g->ws_ready = true;
@@ -233,6 +341,7 @@ void free_graph(gbs_graph *g) {
     if (!g) return;
     cudaFree(g->d_row);
     cudaFree(g->d_adj);
+    cudaFree(g->d_w64);
     cudaFree(g->ws.mid);
     cudaFree(g->ws.trace);
     free_workspace(g->ws);
@@ -251,6 +360,8 @@ double default_delta(double max_w, uint32_t n, uint64_t m) {
     const double d = max_w / avg;
     return d > 0 ? d : 1.0;
 }
+
+size_t dist_bytes(gbs_weight_type wt) { return wt == GBS_WEIGHT_F64 ? 8 : 4; }
 
 uint32_t max_weight_bits(gbs_weight_type wt, double max_w) {
     if (wt == GBS_WEIGHT_U32) return (uint32_t)max_w;
@@ -273,6 +384,17 @@ Resolved resolve_schedule(gbs_weight_type wt, double max_w, uint32_t n, uint64_t
         r.light_bits = (uint32_t)std::min(std::max(fl, 0.0), 4294967295.0);
         r.light = r.light_bits;
         r.inv_delta_f = 0.f;
+        r.light_key = r.light_bits;
+    } else if (wt == GBS_WEIGHT_F64) {
+        r.delta = delta;
+        r.inv_delta_d = 1.0 / delta;
+        r.inv_delta_f = (float)r.inv_delta_d;
+        if (light < 0) light = delta;
+        if (std::isinf(light)) light = 1.7976931348623157e308;
+        r.light = light;
+        std::memcpy(&r.light_key, &light, 8);
+        r.light_bits = 0;
+        r.delta_u = 1;
     } else {
         r.delta = delta;
         r.inv_delta_f = (float)(1.0 / delta);
@@ -286,6 +408,7 @@ Resolved resolve_schedule(gbs_weight_type wt, double max_w, uint32_t n, uint64_t
         r.light_bits = bits;
         r.light = lf;
         r.delta_u = 1;
+        r.light_key = bits;
     }
     return r;
 }
@@ -322,7 +445,7 @@ void graph_features(const gbs_graph *g, float *f) {
     f[3] = g->max_w > 0 ? (float)(g->mean_w / g->max_w) : 0.f;
 }
 
-gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t *dist_dev,
+gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_dev,
                       int32_t *pred_dev, gbs_stats *stats, bool learned, bool *guard_hit) {
     if (src >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
     if (guard_hit) *guard_hit = false;
@@ -361,10 +484,15 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     cudaStream_t s = g->stream;
     const int tb = 256;
     const int eb = std::max(1, std::min<int>((g->n + tb - 1) / tb, g->sms * 8));
-    if (!g->mid_valid || g->mid_light_bits != r.light_bits) {
-        st = launch_mid(g->d_row, g->d_adj, g->n, r.light_bits, g->ws.mid, g->sms, s);
-        if (st != GBS_OK) return st;
-        g->mid_light_bits = r.light_bits;
+    if (!g->mid_valid || g->mid_light_key != r.light_key) {
+        if (g->wtype == GBS_WEIGHT_F64) {
+            k_mid64<<<eb, tb, 0, s>>>(g->d_row, g->d_w64, g->n, r.light_key, g->ws.mid);
+            GBS_CUDA(cudaGetLastError());
+        } else {
+            st = launch_mid(g->d_row, g->d_adj, g->n, r.light_bits, g->ws.mid, g->sms, s);
+            if (st != GBS_OK) return st;
+        }
+        g->mid_light_key = r.light_key;
         g->mid_valid = true;
     }
     if (g->epoch > 0xF0000000u || g->hround > 0xF0000000u) {
@@ -385,12 +513,15 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
     a.hround0 = g->hround;
     a.delta_u = r.delta_u;
     a.inv_delta_f = r.inv_delta_f;
+    a.inv_delta_d = r.inv_delta_d;
+    a.g.w64 = g->d_w64;
     a.wait_ns = (unsigned long long)((p && p->wait_limit_ms) ? p->wait_limit_ms : 4000u) * 1000000ull;
     a.flags = p ? p->flags : 0u;
     const bool no_solo = (a.flags & GBS_F_NO_SOLO) != 0;
     a.solo_items = no_solo ? 0u : ((p && p->solo_entries) ? p->solo_entries : 1024u);
     a.solo_desc = no_solo ? 0u : ((p && p->solo_descs) ? p->solo_descs : 64u);
-    a.no_heavy = r.light_bits >= max_weight_bits(g->wtype, g->max_w) ? 1u : 0u;
+    a.no_heavy = (g->wtype == GBS_WEIGHT_F64 ? r.light >= g->max_w
+                                             : r.light_bits >= max_weight_bits(g->wtype, g->max_w)) ? 1u : 0u;
     a.inline_max = (p && p->inline_edges) ? p->inline_edges : kInlineEdges;
     a.run_ns = a.wait_ns * 16ull;
     a.ctrl = learned ? kCtrlLearned : kCtrlFixed;
@@ -423,19 +554,29 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
 
     GBS_CUDA(cudaEventRecord(g->ev[0], s));
     GBS_CUDA(cudaMemsetAsync(g->ws.ctl, 0, sizeof(Ctl), s));
-    k_reset<<<eb, tb, 0, s>>>(g->ws.dp, g->ws.tag, g->n, src, g->ws.ring, g->ws.ctl, span0, full0);
+    const unsigned long long src_word = g->wtype == GBS_WEIGHT_F64 ? 0ull : (unsigned long long)src;
+    k_reset<<<eb, tb, 0, s>>>(g->ws.dp, g->ws.tag, g->n, src, src_word, g->ws.ring, g->ws.ctl, span0, full0);
     GBS_CUDA(cudaGetLastError());
     GBS_CUDA(cudaEventRecord(g->ev[1], s));
     void *args[] = {&a};
-    const void *kfn = g->wtype == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<true>
-                                                 : (const void *)sssp_persistent<false>;
+    const void *kfn = g->wtype == GBS_WEIGHT_F64   ? (const void *)sssp_persistent<kWF64>
+                      : g->wtype == GBS_WEIGHT_F32 ? (const void *)sssp_persistent<kWF32>
+                                                   : (const void *)sssp_persistent<kWU32>;
     GBS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(g->blocks), dim3(kTPB), args, 0, s));
     GBS_CUDA(cudaEventRecord(g->ev[2], s));
     if (dist_dev || pred_dev) {
-        if (g->wtype == GBS_WEIGHT_F32)
-            k_unpack<true><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, dist_dev, pred_dev);
-        else
-            k_unpack<false><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, dist_dev, pred_dev);
+        if (g->wtype == GBS_WEIGHT_F64) {
+            k_unpack64<<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, static_cast<unsigned long long *>(dist_dev), pred_dev);
+            GBS_CUDA(cudaGetLastError());
+            if (pred_dev) {
+                k_pred64<<<g->sms * 8, 256, 0, s>>>(g->d_row, g->d_adj, g->d_w64, g->ws.dp, g->n, src, pred_dev);
+                GBS_CUDA(cudaGetLastError());
+            }
+        } else if (g->wtype == GBS_WEIGHT_F32) {
+            k_unpack<true><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, static_cast<uint32_t *>(dist_dev), pred_dev);
+        } else {
+            k_unpack<false><<<eb, tb, 0, s>>>(g->ws.dp, g->n, src, static_cast<uint32_t *>(dist_dev), pred_dev);
+        }
         GBS_CUDA(cudaGetLastError());
     }
     GBS_CUDA(cudaEventRecord(g->ev[3], s));
@@ -501,7 +642,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t 
 // schedule; a learned run that passes (1 + margin) x that time stops, the
 // plain schedule runs instead, and later learned calls on the graph run the
 // plain schedule directly.  Reported times include every run the call made.
-gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, uint32_t *dist_dev, int32_t *pred_dev,
+gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_dev, int32_t *pred_dev,
                     gbs_stats *stats) {
     const bool learned = p && (p->flags & GBS_F_LEARNED);
     if (!learned) return launch_run(g, src, p, dist_dev, pred_dev, stats, false, nullptr);
@@ -587,11 +728,14 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
     std::vector<uint32_t> row32;
     std::vector<uint2> adj;
     double max_w = 0.0;
-    gbs_status st = prepare_csr(n, m, row_offsets, cols, weights, wtype, row32, adj, max_w);
+    std::vector<unsigned long long> w64;
+    gbs_status st = prepare_csr(n, m, row_offsets, cols, weights, wtype, row32, adj, max_w, &w64);
     if (st != GBS_OK) return st;
     double wsum = 0.0;
     for (uint64_t e = 0; e < m; ++e)
-        wsum += wtype == GBS_WEIGHT_U32 ? (double)((const uint32_t *)weights)[e] : (double)((const float *)weights)[e];
+        wsum += wtype == GBS_WEIGHT_U32   ? (double)((const uint32_t *)weights)[e]
+                : wtype == GBS_WEIGHT_F32 ? (double)((const float *)weights)[e]
+                                          : ((const double *)weights)[e];
     int dev = 0;
     GBS_CUDA(cudaGetDevice(&dev));
     gbs_graph *g = new gbs_graph();
@@ -618,7 +762,11 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
         (e = cudaMemcpy(g->d_row, row32.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice)) !=
             cudaSuccess ||
         (m && (e = cudaMemcpy(g->d_adj, adj.data(), sizeof(uint2) * m, cudaMemcpyHostToDevice)) !=
-                  cudaSuccess)) {
+                  cudaSuccess) ||
+        (wtype == GBS_WEIGHT_F64 &&
+         ((e = cudaMalloc(&g->d_w64, sizeof(unsigned long long) * (m ? m : 1))) != cudaSuccess ||
+          (m && (e = cudaMemcpy(g->d_w64, w64.data(), sizeof(unsigned long long) * m, cudaMemcpyHostToDevice)) !=
+                    cudaSuccess)))) {
         free_graph(g);
         return fail(e == cudaErrorMemoryAllocation ? GBS_ERR_NO_MEMORY : GBS_ERR_CUDA, cudaGetErrorString(e));
     }
@@ -647,7 +795,7 @@ gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m, gbs_weig
 gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_dev,
                            int32_t *pred_dev, gbs_stats *stats) {
     if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
-    return run_sssp(g, source, params, (uint32_t *)dist_dev, pred_dev, stats);
+    return run_sssp(g, source, params, dist_dev, pred_dev, stats);
 }
 
 gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_out,
@@ -659,7 +807,7 @@ gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, voi
                     stats);
     if (st != GBS_OK) return st;
     if (dist_out)
-        GBS_CUDA(cudaMemcpyAsync(dist_out, g->d_dist, sizeof(uint32_t) * g->n, cudaMemcpyDeviceToHost,
+        GBS_CUDA(cudaMemcpyAsync(dist_out, g->d_dist, dist_bytes(g->wtype) * g->n, cudaMemcpyDeviceToHost,
                                  g->stream));
     if (pred_out)
         GBS_CUDA(cudaMemcpyAsync(pred_out, g->d_pred, sizeof(int32_t) * g->n, cudaMemcpyDeviceToHost,
@@ -674,7 +822,7 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k, con
     gbs_stats total{};
     for (uint32_t i = 0; i < k; ++i) {
         gbs_stats one{};
-        void *d = dist_out ? (void *)((uint32_t *)dist_out + (size_t)i * g->n) : nullptr;
+        void *d = dist_out ? (void *)((char *)dist_out + dist_bytes(g->wtype) * (size_t)i * g->n) : nullptr;
         int32_t *pr = pred_out ? pred_out + (size_t)i * g->n : nullptr;
         gbs_status st = gbs_sssp(g, sources[i], params, d, pr, &one);
         if (st != GBS_OK) return st;

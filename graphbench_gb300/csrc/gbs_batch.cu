@@ -150,7 +150,7 @@ uint32_t auto_group_ctas(uint32_t count, uint32_t blocks) {
 gbs_status build_plan(gbs_plan *p, const gbs_batch_params *bp, int sms, uint32_t n_cap, uint64_t m_cap,
                       std::vector<InstDesc> &inst) {
     p->count = (uint32_t)inst.size();
-    const int per_sm = persistent_ctas_per_sm(p->f32, true);
+    const int per_sm = persistent_ctas_per_sm(p->f32 ? GBS_WEIGHT_F32 : GBS_WEIGHT_U32, true);
     if (per_sm < 1) return fail(GBS_ERR_UNSUPPORTED, "batched kernel cannot be resident");
     const uint32_t max_blocks = (uint32_t)(per_sm * sms);
     uint32_t gc = (bp && bp->group_ctas) ? bp->group_ctas : auto_group_ctas(p->count, max_blocks);
@@ -212,8 +212,8 @@ gbs_status build_plan(gbs_plan *p, const gbs_batch_params *bp, int sms, uint32_t
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         const Workspace *wsp = p->d_ws;
-        e = p->f32 ? cudaLaunchKernelEx(&cfg, sssp_batch<true>, a, wsp)
-                   : cudaLaunchKernelEx(&cfg, sssp_batch<false>, a, wsp);
+        e = p->f32 ? cudaLaunchKernelEx(&cfg, sssp_batch<kWF32>, a, wsp)
+                   : cudaLaunchKernelEx(&cfg, sssp_batch<kWU32>, a, wsp);
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t e_end = cudaStreamEndCapture(p->stream, &graph);
@@ -263,6 +263,8 @@ gbs_status gbs_pack_create(uint32_t count, const gbs_csr_view *graphs, gbs_weigh
     if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     if (count == 0 || !graphs) return fail(GBS_ERR_INVALID_ARG, "empty pack");
+    if (wtype != GBS_WEIGHT_U32 && wtype != GBS_WEIGHT_F32)
+        return fail(GBS_ERR_UNSUPPORTED, "packs take uint32 or float32 graphs");
     gbs_pack *p = new gbs_pack();
     p->count = count;
     p->wtype = wtype;
@@ -330,6 +332,7 @@ gbs_status gbs_plan_sources(gbs_graph *g, const uint32_t *sources, uint32_t k, c
     if (!out) return fail(GBS_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     if (!g || !sources || k == 0) return fail(GBS_ERR_INVALID_ARG, "graph, sources and k > 0 are required");
+    if (g->wtype == GBS_WEIGHT_F64) return fail(GBS_ERR_UNSUPPORTED, "plans take uint32 or float32 graphs");
     for (uint32_t i = 0; i < k; ++i)
         if (sources[i] >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
     gbs_plan *p = nullptr;

@@ -39,12 +39,13 @@ struct gbs_graph {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     uint32_t *d_row = nullptr;
     uint2 *d_adj = nullptr;
+    unsigned long long *d_w64 = nullptr;    // float64 graphs: weights in adj order
     // workspace
     bool ws_ready = false;
     gbs::Workspace ws{};
     uint32_t *d_dist = nullptr;
     int32_t *d_pred = nullptr;
-    uint32_t mid_light_bits = 0;
+    unsigned long long mid_light_key = 0;   // light bound the cached split index was built for
     bool mid_valid = false;
     uint32_t epoch = 1, hround = 1;
     uint32_t trace_n = 0;
@@ -69,7 +70,12 @@ struct Resolved {
     double delta, light;
     uint32_t delta_u, light_bits;
     float inv_delta_f;
+    double inv_delta_d;                 // float64 graphs
+    unsigned long long light_key;       // bits of the light bound in the weight type
 };
+
+// Bytes of one distance in the weight type (4, or 8 for float64).
+size_t dist_bytes(gbs_weight_type wt);
 
 // max weight / average out-degree (1 for an empty graph).
 double default_delta(double max_w, uint32_t n, uint64_t m);
@@ -85,9 +91,10 @@ void sort_rows(const uint64_t *row, const uint32_t *cols, const uint32_t *wbits,
 // Validates a host CSR (offsets, targets, weights: finite and >= 0 for
 // float32, -0 stored as +0) and returns its uint32 offsets, its rows sorted
 // by (weight, col) as {col, weight bits} and its largest weight.
+// float64 weights (w64 given) keep adj = {col, 0} and the weights in w64.
 gbs_status prepare_csr(uint32_t n, uint64_t m, const uint64_t *row_offsets, const uint32_t *cols,
                        const void *weights, gbs_weight_type wtype, std::vector<uint32_t> &row32,
-                       std::vector<uint2> &adj, double &max_w);
+                       std::vector<uint2> &adj, double &max_w, std::vector<unsigned long long> *w64 = nullptr);
 
 // Launches the first-heavy-edge search: mid[v] = first edge of row v whose
 // weight bits exceed light_bits.
@@ -101,6 +108,6 @@ gbs_status alloc_workspace(Workspace &w, uint32_t n_cap, uint64_t m_cap, cudaStr
 void free_workspace(Workspace &w);
 
 // Resident CTAs of the persistent kernels on one SM (0 if they cannot run).
-int persistent_ctas_per_sm(bool f32, bool batch);
+int persistent_ctas_per_sm(gbs_weight_type wt, bool batch);
 
 }  // namespace gbs

@@ -133,6 +133,7 @@ struct DevGraph {
     gbs_weight_type wtype;
     const uint32_t *row;
     const uint2 *adj;
+    const unsigned long long *w64;   // float64 graphs: the weights (adj holds the targets)
 };
 
 struct Workspace {
@@ -191,6 +192,7 @@ struct SsspArgs {
     uint32_t hround0;       // first heavy-round stamp of this run
     uint32_t delta_u;       // uint32 bucket width (>= 1)
     float inv_delta_f;      // float32: bucket = floor(d * inv_delta)
+    double inv_delta_d;     // float64: bucket = floor(d * inv_delta)
     uint32_t flags;         // GBS_F_* of the call
     uint32_t solo_items;    // a SCAN/PENDING phase with at most this many entries runs on one CTA
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA

@@ -133,9 +133,9 @@ gbs_status setup_device(int dev, DeviceSetup **out) {
         if (e != cudaSuccess) return na_fail(GBS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         int per_u = 0, per_f = 0;
         if ((e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_u, sssp_persistent<false>, kTPB, 0)) !=
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_u, sssp_persistent<kWU32>, kTPB, 0)) !=
                 cudaSuccess ||
-            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, sssp_persistent<true>, kTPB, 0)) !=
+            (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, sssp_persistent<kWF32>, kTPB, 0)) !=
                 cudaSuccess)
             return na_fail(GBS_ERR_CUDA, cudaGetErrorString(e));
         if (per_u < 1 || per_f < 1) return na_fail(GBS_ERR_UNSUPPORTED, "persistent kernel cannot be resident");
@@ -251,10 +251,10 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     NA_CUDA(cudaGetLastError());
     void *args[] = {&a};
     if (f32)
-        NA_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent<true>, dim3(d->blocks_f32), dim3(kTPB),
+        NA_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent<kWF32>, dim3(d->blocks_f32), dim3(kTPB),
                                             args, 0, s));
     else
-        NA_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent<false>, dim3(d->blocks_u32), dim3(kTPB),
+        NA_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent<kWU32>, dim3(d->blocks_u32), dim3(kTPB),
                                             args, 0, s));
     if (f32)
         k_noalloc_unpack<true><<<eb, tb, 0, s>>>(a.ws.dp, n, source, (uint32_t *)dist_dev, pred_dev);

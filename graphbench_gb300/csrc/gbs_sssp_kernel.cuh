@@ -71,13 +71,51 @@ struct Uniform {
     unsigned long long t0;  // globaltimer at kernel entry (per CTA)
 };
 
-template <bool F32>
-__device__ __forceinline__ uint32_t bucket_of(uint32_t dbits, const SsspArgs &a) {
-    if (F32) {
-        float q = floorf(__fmul_rn(__uint_as_float(dbits), a.inv_delta_f));
+// Arithmetic of a run: uint32 weights (exact sums, overflow reported),
+// float32 (one rounding per relaxation) or float64 (one rounding in double,
+// the reference's own arithmetic).  uint32 and float32 distances share one
+// 64-bit word with the predecessor ((dist << 32) | pred); float64 distances
+// fill the word (non-negative doubles order like their bit patterns) and the
+// predecessor is found after the run.
+enum : int { kWU32 = 0, kWF32 = 1, kWF64 = 2 };
+template <int WT> struct Arith {
+    using D = uint32_t;            // distance bits
+    using Wt = uint32_t;           // weight bits
+};
+template <> struct Arith<kWF64> {
+    using D = unsigned long long;
+    using Wt = unsigned long long;
+};
+
+template <int WT>
+__device__ __forceinline__ typename Arith<WT>::D dist_of(unsigned long long p) {
+    if constexpr (WT == kWF64) return p;
+    else return (uint32_t)(p >> 32);
+}
+
+template <int WT>
+__device__ __forceinline__ unsigned long long pack_dist(typename Arith<WT>::D d, uint32_t u) {
+    if constexpr (WT == kWF64) return d;
+    else return ((unsigned long long)d << 32) | u;
+}
+
+// Weight of edge e whose {col, weight bits} word is ew.
+template <int WT>
+__device__ __forceinline__ typename Arith<WT>::Wt weight_at(const SsspArgs &a, uint32_t e, uint2 ew) {
+    if constexpr (WT == kWF64) return __ldg(a.g.w64 + e);
+    else return ew.y;
+}
+
+template <int WT>
+__device__ __forceinline__ uint32_t bucket_of(typename Arith<WT>::D d, const SsspArgs &a) {
+    if constexpr (WT == kWF64) {
+        const double q = floor(__dmul_rn(__longlong_as_double((long long)d), a.inv_delta_d));
+        return q >= 4294967040.0 ? kBucketMax : (uint32_t)q;
+    } else if constexpr (WT == kWF32) {
+        float q = floorf(__fmul_rn(__uint_as_float(d), a.inv_delta_f));
         return q >= 4294967040.0f ? kBucketMax : (uint32_t)q;
     } else {
-        uint32_t q = dbits / a.delta_u;
+        uint32_t q = d / a.delta_u;
         return q > kBucketMax ? kBucketMax : q;
     }
 }
@@ -89,8 +127,9 @@ constexpr int kCand = 64;          // candidate buffer: < 32 kept + <= 32 per ap
 struct WarpScratch {
     uint32_t bins[2 * kQueues];    // enqueue histogram and list bases
     uint32_t cv[kCand];            // candidate target
-    uint32_t cnd[kCand];           // candidate tentative distance bits
-    uint32_t cu[kCand];            // candidate source
+    uint32_t cnd[kCand];           // candidate tentative distance bits (low word)
+    uint32_t cu[kCand];            // candidate source; float64 runs: distance high word
+                                   // (their predecessors are found after the run)
 };
 
 // Targets of one phase's appends.
@@ -176,16 +215,22 @@ __device__ __forceinline__ void warp_append(uint32_t *buf, uint32_t *cnt, uint32
     }
 }
 
-// Tentative distance of an edge (u32: overflow check; f32: one rounding).
-template <bool F32>
-__device__ __forceinline__ bool edge_sum(uint32_t du, uint32_t wbits, uint32_t &nd) {
-    if (F32) {
+// Tentative distance of an edge (u32: overflow check; f32 / f64: one rounding).
+template <int WT>
+__device__ __forceinline__ bool edge_sum(typename Arith<WT>::D du, typename Arith<WT>::Wt wbits,
+                                         typename Arith<WT>::D &nd) {
+    if constexpr (WT == kWF64) {
+        nd = (unsigned long long)__double_as_longlong(
+            __dadd_rn(__longlong_as_double((long long)du), __longlong_as_double((long long)wbits)));
+        return true;
+    } else if constexpr (WT == kWF32) {
         nd = __float_as_uint(__fadd_rn(__uint_as_float(du), __uint_as_float(wbits)));
         return true;
+    } else {
+        const unsigned long long s = (unsigned long long)du + wbits;
+        nd = (uint32_t)s;
+        return s < 0xFFFFFFFFull;
     }
-    const unsigned long long s = (unsigned long long)du + wbits;
-    nd = (uint32_t)s;
-    return s < 0xFFFFFFFFull;
 }
 
 // Relaxes U candidate edges (u[j] -> v[j], tentative distance nd[j],
@@ -195,21 +240,20 @@ __device__ __forceinline__ bool edge_sum(uint32_t du, uint32_t wbits, uint32_t &
 //   1. packed (dist << 32 | pred) atomicMin: did the distance drop?
 //   2. dedup: same bucket -> frontier stamp; window -> smallest queued
 //      bucket (tag); beyond the window -> pending (tag = kTagPending)
-template <bool F32, int U>
+template <int WT, int U>
 __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &t, const bool (&cand)[U],
                                               const uint32_t (&v)[U], const uint32_t (&uo)[U],
-                                              const uint32_t (&nd)[U], int (&q)[U], uint32_t &imp) {
+                                              const typename Arith<WT>::D (&nd)[U], int (&q)[U], uint32_t &imp) {
     unsigned long long old[U];
 #pragma unroll
-    for (int j = 0; j < U; ++j)
-        old[j] = cand[j] ? atomicMin(a.ws.dp + v[j], ((unsigned long long)nd[j] << 32) | uo[j]) : 0ull;
+    for (int j = 0; j < U; ++j) old[j] = cand[j] ? atomicMin(a.ws.dp + v[j], pack_dist<WT>(nd[j], uo[j])) : 0ull;
     uint32_t nb[U], kind[U], r[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) {
-        const unsigned long long packed = ((unsigned long long)nd[j] << 32) | uo[j];
-        const bool dec = cand[j] && packed < old[j] && nd[j] < (uint32_t)(old[j] >> 32);
+        const unsigned long long packed = pack_dist<WT>(nd[j], uo[j]);
+        const bool dec = cand[j] && packed < old[j] && nd[j] < dist_of<WT>(old[j]);
         imp += dec ? 1u : 0u;
-        nb[j] = dec ? bucket_of<F32>(nd[j], a) : 0u;
+        nb[j] = dec ? bucket_of<WT>(nd[j], a) : 0u;
         kind[j] = !dec ? 0u
                 : nb[j] < t.cur_hi ? 1u
                 : (unsigned long long)nb[j] < (unsigned long long)t.W + kNB ? 2u : 3u;
@@ -240,7 +284,7 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
 // targets and weights are loaded (val[j] = the lane has an edge in slot j).
 // Runs the atomic part (improve_batch + enqueue) on the top `take` (<= 32)
 // candidates of the warp's buffer, one per lane.
-template <bool F32>
+template <int WT>
 __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t take,
                                            uint32_t &imp) {
     const unsigned lane = lane_id();
@@ -249,12 +293,18 @@ __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, 
     const uint32_t i = nc - take + lane;
     uint32_t v1[1] = {has ? s->cv[i] : 0u};
     uint32_t u1[1] = {has ? s->cu[i] : 0u};
-    uint32_t n1[1] = {has ? s->cnd[i] : 0u};
+    typename Arith<WT>::D n1[1];
+    if constexpr (WT == kWF64) {
+        n1[0] = has ? (((unsigned long long)s->cu[i] << 32) | s->cnd[i]) : 0ull;
+        u1[0] = 0u;
+    } else {
+        n1[0] = has ? s->cnd[i] : 0u;
+    }
     const bool c1[1] = {has};
     __syncwarp();
     nc -= take;
     int q[1];
-    improve_batch<F32, 1>(a, t, c1, v1, u1, n1, q, imp);
+    improve_batch<WT, 1>(a, t, c1, v1, u1, n1, q, imp);
     warp_enqueue<1>(a, t, q, v1);
 }
 
@@ -263,10 +313,10 @@ __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, 
 // Only edges that pass the read-only filter (packed tentative value below
 // the current dp) become candidates; they collect in the warp's shared-memory
 // buffer and the atomic chain runs once per 32 of them, not once per round.
-template <bool F32, int U>
+template <int WT, int U>
 __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Targets &t, const bool (&val)[U],
-                                                 const uint32_t (&v)[U], const uint32_t (&w)[U],
-                                                 const uint32_t (&uo)[U], const uint32_t (&duo)[U],
+                                                 const uint32_t (&v)[U], const typename Arith<WT>::Wt (&w)[U],
+                                                 const uint32_t (&uo)[U], const typename Arith<WT>::D (&duo)[U],
                                                  uint32_t &nc, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
@@ -277,37 +327,39 @@ __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Target
 #pragma unroll
     for (int j = 0; j < U; ++j) {
         bool cand = false;
-        uint32_t nd = 0;
+        typename Arith<WT>::D nd = 0;
         if (val[j]) {
-            if (!edge_sum<F32>(duo[j], w[j], nd)) atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
-            else cand = (((unsigned long long)nd << 32) | uo[j]) < cur[j];
+            if (!edge_sum<WT>(duo[j], w[j], nd)) atomicExch(&a.ws.ctl->error, (uint32_t)kErrOverflow);
+            else cand = pack_dist<WT>(nd, uo[j]) < cur[j];
         }
         const unsigned m = __ballot_sync(FULL, cand);
         if (m) {
             if (cand) {
                 const uint32_t p = nc + (uint32_t)__popc(m & ((1u << lane) - 1u));
                 s->cv[p] = v[j];
-                s->cnd[p] = nd;
-                s->cu[p] = uo[j];
+                s->cnd[p] = (uint32_t)nd;
+                if constexpr (WT == kWF64) s->cu[p] = (uint32_t)(nd >> 32);
+                else s->cu[p] = uo[j];
             }
             nc += (uint32_t)__popc(m);
             __syncwarp();
-            if (nc >= 32u) cand_flush<F32>(a, t, nc, 32u, imp);
+            if (nc >= 32u) cand_flush<WT>(a, t, nc, 32u, imp);
         }
     }
 }
 
 // Drains the warp's candidate buffer (end of a phase's relaxation work).
-template <bool F32>
+template <int WT>
 __device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t &imp) {
-    if (nc) cand_flush<F32>(a, t, nc, nc, imp);
+    if (nc) cand_flush<WT>(a, t, nc, nc, imp);
 }
 
 // Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
 // given by every lane (len may be 0), kUnroll x 32 edges per round.
-template <bool F32>
-__device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t, uint32_t u, uint32_t du,
-                                            uint32_t s, uint32_t len, uint32_t &nc, uint32_t &imp) {
+template <int WT>
+__device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t, uint32_t u,
+                                            typename Arith<WT>::D du, uint32_t s, uint32_t len, uint32_t &nc,
+                                            uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     uint32_t incl = len;
@@ -319,7 +371,9 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
     const uint32_t total = __shfl_sync(FULL, incl, 31);
     const uint32_t excl = incl - len;
     for (uint32_t k0 = 0; k0 < total; k0 += 32u * kUnroll) {
-        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+        uint32_t v[kUnroll], uo[kUnroll];
+        typename Arith<WT>::Wt w[kUnroll];
+        typename Arith<WT>::D duo[kUnroll];
         bool val[kUnroll];
 #pragma unroll
         for (int j = 0; j < kUnroll; ++j) {
@@ -339,12 +393,13 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
             v[j] = 0;
             w[j] = 0;
             if (val[j]) {
-                const uint2 ew = ld_stream(a.g.adj + so + (k - exo));
+                const uint32_t e = so + (k - exo);
+                const uint2 ew = ld_stream(a.g.adj + e);
                 v[j] = ew.x;
-                w[j] = ew.y;
+                w[j] = weight_at<WT>(a, e, ew);
             }
         }
-        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
+        relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
     }
 }
 

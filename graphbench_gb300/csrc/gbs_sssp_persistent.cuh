@@ -52,7 +52,7 @@ __device__ __forceinline__ Exec cta_exec() {
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
 // A light scan relaxes the row prefix [row, mid), or the whole row when full;
 // a heavy scan the rest [mid, end).
-template <bool F32>
+template <int WT>
 __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x, const uint32_t *F,
                               uint32_t count, uint32_t vtag, bool light, bool full, bool add_s, uint32_t hround,
                               uint32_t &imp) {
@@ -64,13 +64,14 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
     uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
         const uint32_t i = base + lane;
-        uint32_t u = 0, du = 0, s = 0, e = 0;
+        uint32_t u = 0, s = 0, e = 0;
+        typename Arith<WT>::D du = 0;
         bool ok = false;
         if (i < count) {
             u = __ldcg(F + i);
             // the tag check and the row reads are independent: issue together
             const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
-            du = (uint32_t)(__ldcg(a.ws.dp + u) >> 32);
+            du = dist_of<WT>(__ldcg(a.ws.dp + u));
             const uint32_t md = full ? __ldg(a.g.row + u + 1) : __ldg(a.ws.mid + u);
             const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
             ok = tg == vtag;
@@ -99,7 +100,9 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             if (pos + nd <= a.ws.desc_cap) {
                 for (uint32_t c = 0; c < nd; ++c) {
                     const uint32_t cs = s + c * kDescEdges;
-                    a.ws.desc[pos + c] = make_uint4(u, du, cs, min(e, cs + kDescEdges));
+                    // float64 distances do not fit the descriptor: the
+                    // relaxation reads dp[u] again (a fresher value is as valid)
+                    a.ws.desc[pos + c] = make_uint4(u, WT == kWF64 ? 0u : (uint32_t)du, cs, min(e, cs + kDescEdges));
                 }
             } else if (nd) {
                 atomicExch(&ctl->error, (uint32_t)kErrCapacity);
@@ -107,11 +110,11 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             my_edges += nd ? len : 0u;
         }
         // short rows: relaxed by this warp now
-        relax_group<F32>(a, t, u, du, s, nd ? 0u : len, nc, imp);
+        relax_group<WT>(a, t, u, du, s, nd ? 0u : len, nc, imp);
         warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n,
                     ok && add_s && hold != hround, u, ctl);
     }
-    cand_drain<F32>(a, t, nc, imp);
+    cand_drain<WT>(a, t, nc, imp);
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
     if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
@@ -119,37 +122,42 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
 
 // ------------------------------------------------------------------ EDGES
 // One warp per descriptor (<= kDescEdges edges of one row = one round).
-template <bool F32>
+template <int WT>
 __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exec &x, uint32_t count,
                                   uint32_t &imp) {
     const unsigned lane = lane_id();
     uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t c = x.warp; c < count; c += x.nwarps) {
         const uint4 d = __ldcg(a.ws.desc + c);
-        uint32_t v[kUnroll], w[kUnroll], uo[kUnroll], duo[kUnroll];
+        typename Arith<WT>::D du;
+        if constexpr (WT == kWF64) du = dist_of<WT>(__ldcg(a.ws.dp + d.x));
+        else du = d.y;
+        uint32_t v[kUnroll], uo[kUnroll];
+        typename Arith<WT>::Wt w[kUnroll];
+        typename Arith<WT>::D duo[kUnroll];
         bool val[kUnroll];
 #pragma unroll
         for (int j = 0; j < kUnroll; ++j) {
             const uint32_t e = d.z + 32u * j + lane;
             val[j] = e < d.w;
             uo[j] = d.x;
-            duo[j] = d.y;
+            duo[j] = du;
             v[j] = 0;
             w[j] = 0;
             if (val[j]) {
                 const uint2 ew = ld_stream(a.g.adj + e);
                 v[j] = ew.x;
-                w[j] = ew.y;
+                w[j] = weight_at<WT>(a, e, ew);
             }
         }
-        relax_candidates<F32>(a, t, val, v, w, uo, duo, nc, imp);
+        relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
     }
-    cand_drain<F32>(a, t, nc, imp);
+    cand_drain<WT>(a, t, nc, imp);
 }
 
 // Moves pending vertices whose bucket entered the window [W, W+kNB) into the
 // ring; the rest go to the other pending list.
-template <bool F32>
+template <int WT>
 __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr) {
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
@@ -172,7 +180,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
             const uint32_t tg = __ldcg(a.ws.tag + v[0]);
             stale += tg != kTagPending ? 1u : 0u;
             if (tg == kTagPending) {
-                const uint32_t nb = bucket_of<F32>((uint32_t)(__ldcg(a.ws.dp + v[0]) >> 32), a);
+                const uint32_t nb = bucket_of<WT>(dist_of<WT>(__ldcg(a.ws.dp + v[0])), a);
                 if ((unsigned long long)nb < (unsigned long long)U.W + kNB) {
                     a.ws.tag[v[0]] = nb;
                     q[0] = 1 + (int)(nb % kNB);
@@ -211,7 +219,7 @@ __device__ inline void init_instance(const SsspArgs &a, const Uniform &U, const 
 
 // FINISH: packed state -> the caller's dist / pred, and the reached vertices
 // and their out-edges (the GTEPS numerator) summed into the control block.
-template <bool F32>
+template <int WT>
 __device__ void finish_instance(const SsspArgs &a, const Exec &x, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const uint32_t n = a.g.n;
@@ -220,7 +228,7 @@ __device__ void finish_instance(const SsspArgs &a, const Exec &x, uint32_t &imp)
     for (uint32_t v = x.tid; v < n; v += x.nthreads) {
         const unsigned long long p = __ldcg(a.ws.dp + v);
         const bool reached = p != kUnreached;
-        if (a.dist_out) a.dist_out[v] = reached ? (uint32_t)(p >> 32) : (F32 ? 0x7F800000u : 0xFFFFFFFFu);
+        if (a.dist_out) a.dist_out[v] = reached ? (uint32_t)(p >> 32) : (WT == kWF32 ? 0x7F800000u : 0xFFFFFFFFu);
         if (a.pred_out) a.pred_out[v] = reached ? (v == a.source ? (int32_t)v : (int32_t)(uint32_t)p) : -1;
         if (reached) {
             ++r;
@@ -242,7 +250,7 @@ __device__ void finish_instance(const SsspArgs &a, const Exec &x, uint32_t &imp)
 }
 
 // Runs the phase U.phase with executor x (grid or one CTA).
-template <bool F32>
+template <int WT>
 __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
                           uint32_t &imp) {
     Ctl *ctl = a.ws.ctl;
@@ -261,32 +269,32 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
             // the other (independent: no barrier between them)
             for (uint32_t j = 0; j < U.span; ++j) {
                 const uint32_t bk = U.b + j;
-                scan_frontier<F32>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n,
+                scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n,
                                    min(__ldcg(&ctl->ring_cnt[bk % kNB].v), n), bk, true, full, !full, U.hround,
                                    imp);
             }
             break;
         case kPhLight:
-            scan_frontier<F32>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
+            scan_frontier<WT>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
                                min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, full, !full,
                                U.hround, imp);
             break;
         case kPhHeavy:
-            scan_frontier<F32>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
+            scan_frontier<WT>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
                                min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), n), kTagInit, false, false, false,
                                U.hround, imp);
             break;
         case kPhEdges:
-            relax_descriptors<F32>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
+            relax_descriptors<WT>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
             break;
         case kPhPending:
-            rebucket_pending<F32>(a, U, x, scr);
+            rebucket_pending<WT>(a, U, x, scr);
             break;
         case kPhInit:
             init_instance(a, U, x);
             break;
         case kPhFinish:
-            finish_instance<F32>(a, x, imp);
+            finish_instance<WT>(a, x, imp);
             break;
         default:
             break;
@@ -720,7 +728,7 @@ __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &
 // published state.  Every wait is bounded by a.wait_ns (globaltimer); on
 // expiry the error word is set and every CTA leaves at its next check.  A
 // solo stretch stops after a.wait_ns / 4 so the waiting CTAs never time out.
-template <bool F32, bool Batch>
+template <int WT, bool Batch>
 __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U, WarpScratch *scr,
                                                    uint32_t &imp) {
     Ctl *ctl = a.ws.ctl;
@@ -756,7 +764,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             const bool solo = s_flag[1] != 0;
             __syncthreads();
             if (!solo) break;
-            run_phase<F32>(a, U, cta_exec(), scr, imp);
+            run_phase<WT>(a, U, cta_exec(), scr, imp);
             // atomics whose result is unused (tag and pend_min minima) are
             // fire-and-forget reductions; each thread waits until its own have
             // reached L2 before the decision reads the counters and tags they
@@ -793,7 +801,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
     U.gen += 1;
 }
 
-template <bool F32>
+template <int WT>
 __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     Ctl *ctl = a.ws.ctl;
     __shared__ WarpScratch s_scr[kTPB / 32];
@@ -813,8 +821,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     U.t0 = globaltimer();
     uint32_t imp = 0;
     while (U.phase != kPhDone) {
-        run_phase<F32>(a, U, group_exec(a), scr, imp);
-        barrier_and_decide<F32, false>(a, U, scr, imp);
+        run_phase<WT>(a, U, group_exec(a), scr, imp);
+        barrier_and_decide<WT, false>(a, U, scr, imp);
     }
     for (int o = 16; o > 0; o >>= 1) imp += __shfl_down_sync(0xffffffffu, imp, o);
     if (lane_id() == 0 && imp) atomicAdd(&ctl->st_improvements, (unsigned long long)imp);
@@ -827,7 +835,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
 // Batched launch: CTA group g (group_ctas CTAs) owns workspace ws_groups[g]
 // and solves instances taken from base.queue until the queue is empty.  The
 // control block of a workspace keeps the last stamps between launches.
-template <bool F32>
+template <int WT>
 __global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Workspace *__restrict__ ws_groups) {
     __shared__ SsspArgs s_a;
     __shared__ WarpScratch s_scr[kTPB / 32];
@@ -873,8 +881,8 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Works
             loaded = U.inst;
             U.t0 = globaltimer();   // the run-time limit applies per instance
         }
-        run_phase<F32>(s_a, U, group_exec(s_a), scr, imp);
-        barrier_and_decide<F32, true>(s_a, U, scr, imp);
+        run_phase<WT>(s_a, U, group_exec(s_a), scr, imp);
+        barrier_and_decide<WT, true>(s_a, U, scr, imp);
     }
     if (group_rank(s_a) == 0 && threadIdx.x == 0) {
         // after an error the stamps in flight are unknown: 0 makes the next

@@ -229,7 +229,7 @@ gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, gbs_batch
 uint32_t batch_blocks(int device) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    return (uint32_t)std::max(1, persistent_ctas_per_sm(false, true) * sms);
+    return (uint32_t)std::max(1, persistent_ctas_per_sm(GBS_WEIGHT_U32, true) * sms);
 }
 
 }  // namespace

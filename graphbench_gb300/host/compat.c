@@ -81,7 +81,10 @@ static int set_status(gbs_status st, const char *fn, const char *why) {
     return -1;
 }
 
-/* The weight type the graph's doubles are exact in, or -1. */
+/* The weight type to run in: uint32 when every weight is an integer (exact,
+ * the same sums as the reference's doubles), float32 when allowed and every
+ * weight is float32-exact, float64 otherwise (the reference's arithmetic);
+ * -1 for a negative or non-finite weight. */
 static int weight_type_of(const t_csr *gs) {
     int all_int = 1, all_f32 = 1;
     for (lint e = 0; e < gs->e_size; ++e) {
@@ -89,10 +92,10 @@ static int weight_type_of(const t_csr *gs) {
         if (!(w >= 0.0) || isinf(w)) return -1;
         if (all_int && !(w == floor(w) && w <= 4294967294.0)) all_int = 0;
         if (all_f32 && (double)(float)w != w) all_f32 = 0;
-        if (!all_int && !all_f32) return -1;
     }
     if (all_int) return GBS_WEIGHT_U32;
-    return all_f32 ? GBS_WEIGHT_F32 : -1;
+    if (all_f32 && g_allow_f32) return GBS_WEIGHT_F32;
+    return GBS_WEIGHT_F64;
 }
 
 static gbs_status convert(const t_csr *gs, gbs_graph **out, gbs_weight_type *wt_out, const char **why) {
@@ -104,16 +107,13 @@ static gbs_status convert(const t_csr *gs, gbs_graph **out, gbs_weight_type *wt_
     if (gs->vet_idx[n - 1] != m) { *why = "vet_idx[v_size-1] != e_size"; return GBS_ERR_INVALID_ARG; }
     const int wt = weight_type_of(gs);
     if (wt < 0) {
-        *why = "edge weights must be integers in [0, 2^32-2] (or float32-exact with gbs_compat_allow_float32)";
-        return GBS_ERR_UNSUPPORTED;
+        *why = "edge weights must be finite and >= 0";
+        return GBS_ERR_INVALID_ARG;
     }
-    if (wt == GBS_WEIGHT_F32 && !g_allow_f32) {
-        *why = "fractional weights: enable float32 arithmetic with gbs_compat_allow_float32(1)";
-        return GBS_ERR_UNSUPPORTED;
-    }
+    const size_t wsize = wt == GBS_WEIGHT_F64 ? 8 : 4;
     uint64_t *row = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(n + 1));
     uint32_t *col = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(m ? m : 1));
-    uint32_t *w = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(m ? m : 1));
+    unsigned char *w = (unsigned char *)malloc(wsize * (size_t)(m ? m : 1));
     gbs_status st = GBS_OK;
     if (!row || !col || !w) {
         st = GBS_ERR_NO_MEMORY;
@@ -140,10 +140,13 @@ static gbs_status convert(const t_csr *gs, gbs_graph **out, gbs_weight_type *wt_
         col[e] = (uint32_t)c;
         const double d = gs->edge_info[e].edge_weight;
         if (wt == GBS_WEIGHT_U32) {
-            w[e] = (uint32_t)d;
-        } else {
+            const uint32_t u = (uint32_t)d;
+            memcpy(w + 4 * (size_t)e, &u, 4);
+        } else if (wt == GBS_WEIGHT_F32) {
             const float f = (float)d;
-            memcpy(&w[e], &f, 4);
+            memcpy(w + 4 * (size_t)e, &f, 4);
+        } else {
+            memcpy(w + 8 * (size_t)e, &d, 8);
         }
     }
     st = gbs_graph_create((uint32_t)n, (uint64_t)m, row, col, w, (gbs_weight_type)wt, out);
@@ -239,7 +242,7 @@ static void run_common(const char *fn, t_csr *gs, p_list *predecesor, lint sourc
     st = lookup(gs, &s, &why);
     if (st != GBS_OK) goto out;
     const lint n = gs->v_size;
-    dist = malloc(4 * (size_t)n);
+    dist = malloc(8 * (size_t)n);
     pred = (int32_t *)malloc(4 * (size_t)n);
     if (!dist || !pred) {
         st = GBS_ERR_NO_MEMORY;
@@ -255,12 +258,13 @@ static void run_common(const char *fn, t_csr *gs, p_list *predecesor, lint sourc
         why = gbs_last_error();
         goto out;
     }
-    const int f32 = s->wt == GBS_WEIGHT_F32;
+    const int f32 = s->wt == GBS_WEIGHT_F32, f64 = s->wt == GBS_WEIGHT_F64;
     const uint32_t *du = (const uint32_t *)dist;
     const float *df = (const float *)dist;
+    const double *dd = (const double *)dist;
     for (lint v = 0; v < n; ++v) {
         if (pred[v] < 0) gs->vet_info[v].weight = INFINITY;
-        else gs->vet_info[v].weight = f32 ? (double)df[v] : (double)du[v];
+        else gs->vet_info[v].weight = f64 ? dd[v] : (f32 ? (double)df[v] : (double)du[v]);
     }
     if (!predecesor) goto out;
     if (!all_tight) {
@@ -296,7 +300,10 @@ static void run_common(const char *fn, t_csr *gs, p_list *predecesor, lint sourc
             if (pred[v] < 0 || last[v] == u || !predecesor[v]) continue;
             const double w = gs->edge_info[e].edge_weight;
             int tight;
-            if (f32) {
+            if (f64) {
+                volatile double sum = dd[u] + w;
+                tight = sum == dd[v];
+            } else if (f32) {
                 volatile float sum = df[u] + (float)w;
                 tight = sum == df[v];
             } else {

@@ -52,7 +52,10 @@ typedef enum gbs_status {
 
 typedef enum gbs_weight_type {
     GBS_WEIGHT_U32 = 0,       /* uint32 weights, uint32 distances (UINT32_MAX = unreached) */
-    GBS_WEIGHT_F32 = 1        /* float32 weights >= 0, float32 distances (+inf = unreached) */
+    GBS_WEIGHT_F32 = 1,       /* float32 weights >= 0, float32 distances (+inf = unreached) */
+    GBS_WEIGHT_F64 = 2        /* float64 weights >= 0, float64 distances (+inf = unreached): the
+                                 reference's own arithmetic (doubles, one rounding per
+                                 relaxation); single-source calls only (not packs or plans) */
 } gbs_weight_type;
 
 typedef struct gbs_graph gbs_graph;

@@ -19,10 +19,12 @@
  *   - the graph is converted once to a device CSR and cached (key: the t_csr
  *     address, its array addresses and sizes, and a sample of its contents);
  *     after changing a t_csr in place call gbs_compat_forget(gs);
- *   - edge weights must be integers in [0, 2^32-2] (computed exactly in
- *     uint32, equal to the reference's double sums), or, after
- *     gbs_compat_allow_float32(1), values exactly representable in float32
- *     (computed in float32 arithmetic: not the reference's double sums);
+ *   - edge weights must be finite and >= 0.  Integer weights in [0, 2^32-2]
+ *     run in uint32 (exact, equal to the reference's double sums); any other
+ *     weights run in float64, the reference's own arithmetic (one rounding
+ *     per relaxation), so the distances equal its doubles bit for bit.
+ *     gbs_compat_allow_float32(1) runs float32-exact weights in float32
+ *     instead (faster, but float32 sums, not the reference's doubles);
  *   - errors print one line to stderr and exit(123), the reference's
  *     ERROR_PRINT behaviour (include/graph.h:74); gbs_compat_set_exit(0) makes
  *     them return instead, with gbs_compat_status() holding the status;
@@ -93,7 +95,7 @@ void run_sspath(t_csr *gs, p_list *predecesor, lint source, double delta);
 /* Library-specific controls (no counterpart in the reference). */
 void gbs_compat_forget(const t_csr *gs);        /* drop the cached device copy of gs */
 void gbs_compat_forget_all(void);
-void gbs_compat_allow_float32(int allow);        /* accept float32-exact fractional weights */
+void gbs_compat_allow_float32(int allow);        /* float32 arithmetic for float32-exact weights */
 void gbs_compat_set_exit(int exit_on_error);     /* 1 (default): exit(123) on error */
 gbs_status gbs_compat_status(void);              /* status of the last call */
 

@@ -54,13 +54,13 @@ def lib() -> ctypes.CDLL:
     if _lib is None:
         build()
         L = ctypes.CDLL(str(LIB_PATH))
-        for name in ("or_dijkstra_u32", "or_dijkstra_f32"):
+        for name in ("or_dijkstra_u32", "or_dijkstra_f32", "or_dijkstra_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _P]
             getattr(L, name).restype = ctypes.c_int
-        for name in ("or_min_tight_pred_u32", "or_min_tight_pred_f32"):
+        for name in ("or_min_tight_pred_u32", "or_min_tight_pred_f32", "or_min_tight_pred_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _P, _P]
             getattr(L, name).restype = ctypes.c_int
-        for name in ("or_check_preds_u32", "or_check_preds_f32"):
+        for name in ("or_check_preds_u32", "or_check_preds_f32", "or_check_preds_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _P, _P]
             getattr(L, name).restype = _i64
         for name in ("or_delta_stepping_u32", "or_delta_stepping_f32", "or_delta_stepping_f64"):
@@ -87,12 +87,15 @@ def _prep(row, col, w):
 
 def dijkstra(row, col, w, src: int) -> np.ndarray:
     """Least-fixpoint distances in the weight type (u32: UINT32_MAX unreached;
-    f32: +inf unreached)."""
+    f32 / f64: +inf unreached)."""
     row, col, w = _prep(row, col, w)
     n = len(row) - 1
     if w.dtype == np.uint32:
         d = np.empty(n, dtype=np.uint32)
         rc = lib().or_dijkstra_u32(n, _ptr(row), _ptr(col), _ptr(w), src, _ptr(d))
+    elif w.dtype == np.float64:
+        d = np.empty(n, dtype=np.float64)
+        rc = lib().or_dijkstra_f64(n, _ptr(row), _ptr(col), _ptr(w), src, _ptr(d))
     else:
         d = np.empty(n, dtype=np.float32)
         rc = lib().or_dijkstra_f32(n, _ptr(row), _ptr(col), _ptr(w.astype(np.float32)), src, _ptr(d))
@@ -129,6 +132,9 @@ def min_tight_pred(row, col, w, src: int, dist) -> np.ndarray:
     if w.dtype == np.uint32:
         lib().or_min_tight_pred_u32(n, _ptr(row), _ptr(col), _ptr(w), src,
                                     _ptr(np.ascontiguousarray(dist, dtype=np.uint32)), _ptr(p))
+    elif w.dtype == np.float64:
+        lib().or_min_tight_pred_f64(n, _ptr(row), _ptr(col), _ptr(w), src,
+                                    _ptr(np.ascontiguousarray(dist, dtype=np.float64)), _ptr(p))
     else:
         lib().or_min_tight_pred_f32(n, _ptr(row), _ptr(col), _ptr(w.astype(np.float32)), src,
                                     _ptr(np.ascontiguousarray(dist, dtype=np.float32)), _ptr(p))
@@ -144,6 +150,9 @@ def check_preds(row, col, w, src: int, dist, pred) -> int:
     if w.dtype == np.uint32:
         return int(lib().or_check_preds_u32(n, _ptr(row), _ptr(col), _ptr(w), src,
                                             _ptr(np.ascontiguousarray(dist, dtype=np.uint32)), _ptr(pred)))
+    if w.dtype == np.float64:
+        return int(lib().or_check_preds_f64(n, _ptr(row), _ptr(col), _ptr(w), src,
+                                            _ptr(np.ascontiguousarray(dist, dtype=np.float64)), _ptr(pred)))
     return int(lib().or_check_preds_f32(n, _ptr(row), _ptr(col), _ptr(w.astype(np.float32)), src,
                                         _ptr(np.ascontiguousarray(dist, dtype=np.float32)), _ptr(pred)))
 

@@ -140,6 +140,36 @@ int or_dijkstra_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
     return rc;
 }
 
+/* float64 weights: every relaxation rounds once in double, as the
+ * reference's relax does (sssp/csr_sspath_array.c:419-421). */
+int or_dijkstra_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                    const double *w, uint32_t src, double *dist) {
+    char *done = (char *)calloc(n ? n : 1, 1);
+    or_heap h = {0};
+    int rc = 0;
+    if (!done) return -1;
+    for (uint32_t v = 0; v < n; v++) dist[v] = INFINITY;
+    dist[src] = 0.0;
+    if (heap_push(&h, 0.0, src)) rc = -1;
+    while (!rc && h.n) {
+        or_hent t = heap_pop(&h);
+        uint32_t u = t.v;
+        if (done[u]) continue;
+        done[u] = 1;
+        double du = dist[u];
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            volatile double nd = du + w[e];
+            uint32_t v = col[e];
+            if (nd < dist[v]) {
+                dist[v] = nd;
+                if (heap_push(&h, nd, v)) { rc = -1; break; }
+            }
+        }
+    }
+    free(h.a); free(done);
+    return rc;
+}
+
 /* --------------------------------------------------------- predecessors */
 int or_min_tight_pred_u32(uint32_t n, const uint64_t *row, const uint32_t *col,
                           const uint32_t *w, uint32_t src, const uint32_t *dist,
@@ -169,6 +199,25 @@ int or_min_tight_pred_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
             uint32_t v = col[e];
             if (v == src) continue;
             volatile float nd = dist[u] + w[e];
+            if (nd == dist[v]) {
+                if (pred[v] < 0 || (uint32_t)pred[v] > u) pred[v] = (int32_t)u;
+            }
+        }
+    }
+    pred[src] = (int32_t)src;
+    return 0;
+}
+
+int or_min_tight_pred_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                          const double *w, uint32_t src, const double *dist,
+                          int32_t *pred) {
+    for (uint32_t v = 0; v < n; v++) pred[v] = -1;
+    for (uint32_t u = 0; u < n; u++) {
+        if (isinf(dist[u])) continue;
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {
+            uint32_t v = col[e];
+            if (v == src) continue;
+            volatile double nd = dist[u] + w[e];
             if (nd == dist[v]) {
                 if (pred[v] < 0 || (uint32_t)pred[v] > u) pred[v] = (int32_t)u;
             }
@@ -210,6 +259,25 @@ int64_t or_check_preds_f32(uint32_t n, const uint64_t *row, const uint32_t *col,
         int ok = 0;
         for (uint64_t e = row[p]; e < row[p + 1]; e++) {
             volatile float nd = dist[p] + w[e];
+            if (col[e] == v && nd == dist[v]) { ok = 1; break; }
+        }
+        bad += !ok;
+    }
+    return bad;
+}
+
+int64_t or_check_preds_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
+                           const double *w, uint32_t src, const double *dist,
+                           const int32_t *pred) {
+    int64_t bad = 0;
+    for (uint32_t v = 0; v < n; v++) {
+        if (v == src) continue;
+        if (isinf(dist[v])) { bad += (pred[v] != -1); continue; }
+        int32_t p = pred[v];
+        if (p < 0 || (uint32_t)p >= n || isinf(dist[p])) { bad++; continue; }
+        int ok = 0;
+        for (uint64_t e = row[p]; e < row[p + 1]; e++) {
+            volatile double nd = dist[p] + w[e];
             if (col[e] == v && nd == dist[v]) { ok = 1; break; }
         }
         bad += !ok;

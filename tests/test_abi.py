@@ -80,9 +80,10 @@ def test_null_arguments(gb):
 
 
 def test_host_mirror_weight_rules(gb):
-    """Fractional doubles that float32 cannot hold are refused instead of
-    being rounded (the reference computes in double)."""
-    gs = gb.TCsr(np.array([1, 1], dtype=np.int64), np.array([1], dtype=np.int64), np.array([0.1]))
-    with pytest.raises(gb.GbsError) as e:
-        gb.run_sspath_arr(gs, 0, 0.4)
-    assert e.value.name == "UNSUPPORTED"
+    """Negative or non-finite double weights are refused before any device
+    work (fractional ones run in float64, the reference's arithmetic)."""
+    for bad in (-0.5, np.nan, np.inf):
+        gs = gb.TCsr(np.array([1, 1], dtype=np.int64), np.array([1], dtype=np.int64), np.array([bad]))
+        with pytest.raises(gb.GbsError) as e:
+            gb.run_sspath_arr(gs, 0, 0.4)
+        assert e.value.name == "INVALID_ARG"

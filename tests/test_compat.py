@@ -110,17 +110,16 @@ def test_compat_driver_links(driver):
     assert driver.exists()
 
 
-def test_compat_rejects_inexact_weights_like_the_reference(driver, tmp_path):
-    """Weights that are neither uint32 integers nor float32 values: the
-    reference's ERROR_PRINT behaviour (message, exit 123), or a status with
+def test_compat_rejects_bad_input_like_the_reference(driver, tmp_path):
+    """A negative or NaN weight, or a source out of range: the reference's
+    ERROR_PRINT behaviour (message, exit 123), or a status with
     gbs_compat_set_exit(0).  Rejected before any device work."""
     row = np.array([0, 1, 2], dtype=np.int64)
     col = np.array([1, 0], dtype=np.int64)
-    w = np.array([0.1, 0.2])
-    r, _ = run_driver(driver, tmp_path, row, col, w, 0, 0.4)
+    r, _ = run_driver(driver, tmp_path, row, col, np.array([0.5, -1.0]), 0, 0.4)
     assert r.returncode == 123 and "Error:" in r.stderr and "run_sspath_arr" in r.stderr
-    r, _ = run_driver(driver, tmp_path, row, col, w, 0, 0.4, extra=("f32", "noexit"))
-    assert r.returncode == 0 and "status 7" in r.stdout
+    r, _ = run_driver(driver, tmp_path, row, col, np.array([np.nan, 1.0]), 0, 0.4, extra=("noexit",))
+    assert r.returncode == 0 and "status 1" in r.stdout
     r, _ = run_driver(driver, tmp_path, row, col, np.array([1.0, 2.0]), 5, 1.0, mode="list", extra=("noexit",))
     assert "status 1" in r.stdout   # source out of range
 
@@ -165,6 +164,32 @@ def test_run_sspath_lists_every_tight_predecessor(driver, tmp_path, gb, orc):
         assert sorted(lists[v]) == want, v
         multi += len(want) > 1
     assert multi > 10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["arr", "list"])
+def test_fractional_weights_match_the_reference_doubles(mode, driver, tmp_path, gb, orc, ref_serial):
+    """Weights like the reference's own reader makes (v_to / v_num,
+    graph/csr.c:42): fractional doubles run in float64 and every distance
+    equals the reference's run_sspath_arr bit for bit."""
+    a = gb.gen_rmat(11, 16, 7)
+    w = a.col.astype(np.float64) / 2048.0 + a.w.astype(np.float64) / 255.0
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    r, out = run_driver(driver, tmp_path, a.row, a.col, w, src, 0.4, mode=mode, reps=2)
+    assert r.returncode == 0 and "status 0" in r.stdout, r.stderr
+    dist, lists = read_output(out, a.n)
+    refd, _ = ref_serial.ref_sssp_arr(a.row, a.col, w, src, 0.4)
+    assert np.array_equal(dist, refd)
+    assert np.array_equal(dist, orc.dijkstra(a.row, a.col, w, src))
+    if mode == "arr":
+        mp = orc.min_tight_pred(a.row, a.col, w, src, dist)
+        for v in range(a.n):
+            assert lists[v] == ([] if v == src or not np.isfinite(dist[v]) else [int(mp[v])])
+    else:
+        off, preds = orc.all_tight_preds(a.row, a.col, w, src, dist)
+        for v in range(a.n):
+            want = sorted(set(preds[off[v]:off[v + 1]].tolist())) if np.isfinite(dist[v]) else []
+            assert sorted(lists[v]) == want, v
 
 
 @pytest.mark.gpu

@@ -1,6 +1,6 @@
 """GPU parity tests: the CUDA path (through the C ABI in libgbsssp.so) against
 the oracle and the committed golden vectors.  Distances must be bit-identical
-(uint32 and float32 alike: the least fixpoint does not depend on the
+(uint32, float32 and float64 alike: the least fixpoint does not depend on the
 relaxation order or the bucket width), and predecessors must equal the
 smallest tight in-neighbour, which the oracle computes independently."""
 import hashlib
@@ -230,6 +230,55 @@ def test_wait_limit_returns_timeout_and_device_recovers(gb, orc):
         d, p, _ = g.sssp(3)
     ref = orc.dijkstra(a.row, a.col, a.w, 3)
     assert np.array_equal(d, ref)
+
+
+def _fractional(a):
+    """Fractional double weights in (0, 2): not float32-exact in general."""
+    return a.col.astype(np.float64) / 3072.0 + a.w.astype(np.float64) / 131.0
+
+
+@pytest.mark.parametrize("delta,light", [(None, None), (0.05, None), (0.4, None), (2.5, None),
+                                         (0.4, 0.0), (0.4, 10.0), (100.0, None)])
+def test_float64_rmat_deltas_and_splits(delta, light, gb, orc):
+    """float64 weights: distances bit-identical to the float64 oracle (one
+    rounding per relaxation, as the reference computes), predecessors the
+    smallest tight in-neighbour found by the pass after the run."""
+    a = gb.gen_rmat(12, 16, 13)
+    w = _fractional(a)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    d, p, st = run_and_check(gb, orc, a.row, a.col, w, src, delta=delta, light=light)
+    assert d.dtype == np.float64 and st["reached"] == int(np.isfinite(d).sum())
+
+
+def test_float64_grid_multi_and_device_outputs(gb, orc):
+    torch = pytest.importorskip("torch")
+    a = gb.gen_grid(40, 56, 5, "f32")
+    w = a.w.astype(np.float64) / 7.0
+    srcs = np.array([0, 17, 2239], dtype=np.uint32)
+    with gb.Graph(a.row, a.col, w) as g:
+        D, P, _ = g.sssp_multi(srcs, want_pred=True)
+        dd = torch.empty(a.n, dtype=torch.float64, device="cuda")
+        pd = torch.empty(a.n, dtype=torch.int32, device="cuda")
+        g.sssp_device(17, dd.data_ptr(), pd.data_ptr())
+        with pytest.raises(gb.GbsError) as e:
+            gb.Plan(g, srcs)
+        assert e.value.name == "UNSUPPORTED"
+    for i, s in enumerate(srcs):
+        ref = orc.dijkstra(a.row, a.col, w, int(s))
+        assert np.array_equal(D[i], ref)
+        assert np.array_equal(P[i], orc.min_tight_pred(a.row, a.col, w, int(s), ref))
+    assert np.array_equal(dd.cpu().numpy(), D[1]) and np.array_equal(pd.cpu().numpy(), P[1])
+
+
+def test_reference_mirror_fractional_weights(gb, orc, ref_serial):
+    """The Python mirror with fractional double weights returns the
+    reference's own run_sspath_arr doubles bit for bit."""
+    a = gb.gen_rmat(11, 16, 8)
+    w = _fractional(a)
+    gs = gb.TCsr(a.row[1:].astype(np.int64), a.col.astype(np.int64), w)
+    out = gb.run_sspath_arr(gs, 17, 0.4)
+    refd, _ = ref_serial.ref_sssp_arr(a.row, a.col, w, 17, 0.4)
+    assert np.array_equal(out, refd)
 
 
 def test_reference_mirror_run_sspath_arr(gb, orc):
