@@ -270,13 +270,13 @@ gbs_status alloc_workspace(Workspace &w, uint32_t n_cap, uint64_t m_cap, cudaStr
     GBS_CUDA(cudaMalloc(&w.hst, sizeof(uint32_t) * n));
     GBS_CUDA(cudaMalloc(&w.ring, sizeof(uint32_t) * n * kNB));
     GBS_CUDA(cudaMalloc(&w.fq, sizeof(uint32_t) * n * 3));
-    GBS_CUDA(cudaMalloc(&w.S, sizeof(uint32_t) * n * 2));
     GBS_CUDA(cudaMalloc(&w.pend, sizeof(uint32_t) * n * 2));
     // a SCAN reads at most n entries and cuts each row into ceil(len/kDescEdges)
     // descriptors, so it emits at most n + m/kDescEdges of them
     const uint64_t cap = (uint64_t)n_cap + m_cap / kDescEdges + 64;
     w.desc_cap = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFF0ull);
     GBS_CUDA(cudaMalloc(&w.desc, sizeof(uint4) * (size_t)w.desc_cap));
+    GBS_CUDA(cudaMalloc(&w.hdesc, sizeof(uint4) * (size_t)w.desc_cap));
     GBS_CUDA(cudaMalloc(&w.ctl, sizeof(Ctl)));
     GBS_CUDA(cudaMemsetAsync(w.fst, 0, sizeof(uint32_t) * n, s));
     GBS_CUDA(cudaMemsetAsync(w.hst, 0, sizeof(uint32_t) * n, s));
@@ -287,7 +287,7 @@ gbs_status alloc_workspace(Workspace &w, uint32_t n_cap, uint64_t m_cap, cudaStr
 
 void free_workspace(Workspace &w) {
     cudaFree(w.dp); cudaFree(w.tag); cudaFree(w.fst); cudaFree(w.hst);
-    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.S); cudaFree(w.pend); cudaFree(w.desc); cudaFree(w.ctl);
+    cudaFree(w.ring); cudaFree(w.fq); cudaFree(w.pend); cudaFree(w.desc); cudaFree(w.hdesc); cudaFree(w.ctl);
     w = Workspace{};
 }
 

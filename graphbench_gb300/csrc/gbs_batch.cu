@@ -106,8 +106,8 @@ size_t workspace_bytes(uint32_t n_cap, uint64_t m_cap, uint32_t *desc_cap) {
     b += 3 * align_up(4 * n);             // tag, fst, hst
     b += align_up(4 * n * kNB);           // ring
     b += align_up(4 * n * 3);             // fq
-    b += 2 * align_up(4 * n * 2);         // S, pend
-    b += align_up(16 * (size_t)*desc_cap);
+    b += align_up(4 * n * 2);             // pend
+    b += 2 * align_up(16 * (size_t)*desc_cap);   // desc, hdesc
     b += align_up(sizeof(Ctl));
     return b;
 }
@@ -127,9 +127,9 @@ Workspace carve(unsigned char *base, uint32_t n_cap, uint32_t desc_cap) {
     w.hst = reinterpret_cast<uint32_t *>(take(4 * n));
     w.ring = reinterpret_cast<uint32_t *>(take(4 * n * kNB));
     w.fq = reinterpret_cast<uint32_t *>(take(4 * n * 3));
-    w.S = reinterpret_cast<uint32_t *>(take(4 * n * 2));
     w.pend = reinterpret_cast<uint32_t *>(take(4 * n * 2));
     w.desc = reinterpret_cast<uint4 *>(take(16 * (size_t)desc_cap));
+    w.hdesc = reinterpret_cast<uint4 *>(take(16 * (size_t)desc_cap));
     w.ctl = reinterpret_cast<Ctl *>(take(sizeof(Ctl)));
     w.desc_cap = desc_cap;
     w.n_cap = n_cap;

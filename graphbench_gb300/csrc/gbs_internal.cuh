@@ -13,13 +13,15 @@
 //                     keeps the smallest predecessor among equal distances.
 //   tag[n]    uint32  smallest bucket the vertex was queued for (ring dedup)
 //   fst[n]    uint32  frontier stamp (dedup inside one light sub-phase)
-//   hst[n]    uint32  heavy-round stamp (dedup of the settled list S)
+//   hst[n]    uint32  heavy-round stamp (a vertex's heavy edges are described
+//                     once per heavy round)
 //   ring      kNB lists of n uint32: bucket b lives in list b % kNB while it is
 //                     inside the window [W, W + kNB)
 //   fq        3 lists of n uint32: current-bucket frontier, rotated per step
-//   S         2 lists of n uint32: vertices settled in the current bucket
 //   pend      2 lists of n uint32: vertices whose bucket is beyond the window
 //   desc      edge descriptors {u, dist(u), first edge, end edge} of one SCAN
+//   hdesc     heavy-edge descriptors {u, -, first, end} of the current heavy
+//             round, written by the light scans, relaxed by HEAVY
 #pragma once
 
 #include <cstdint>
@@ -108,7 +110,7 @@ struct __align__(128) Ctl {
     uint32_t pad2[19];
     Line ring_cnt[kNB];
     Line fq_cnt[3];
-    Line s_cnt[2];
+    Line hdesc_cnt;
     Line pend_cnt[2];
     Line pend_min[2];
     Line desc_cnt;
@@ -139,8 +141,9 @@ struct DevGraph {
 struct Workspace {
     unsigned long long *dp;
     uint32_t *tag, *fst, *hst, *mid;
-    uint32_t *ring, *fq, *S, *pend;
+    uint32_t *ring, *fq, *pend;
     uint4 *desc;
+    uint4 *hdesc;           // heavy-edge descriptors (capacity desc_cap)
     uint32_t desc_cap;
     uint32_t n_cap;         // vertices the per-vertex arrays hold (lists use the
                             // instance's n as their stride, n <= n_cap)

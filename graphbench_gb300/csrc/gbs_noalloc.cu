@@ -51,8 +51,7 @@ constexpr size_t kOffFst = al256(kOffTag + 4 * kN);
 constexpr size_t kOffHst = al256(kOffFst + 4 * kN);
 constexpr size_t kOffRing = al256(kOffHst + 4 * kN);
 constexpr size_t kOffFq = al256(kOffRing + 4 * kN * kNB);
-constexpr size_t kOffS = al256(kOffFq + 4 * kN * 3);
-constexpr size_t kOffPend = al256(kOffS + 4 * kN * 2);
+constexpr size_t kOffPend = al256(kOffFq + 4 * kN * 3);
 constexpr size_t kOffDesc = al256(kOffPend + 4 * kN * 2);
 constexpr size_t kOffCheck = al256(kOffDesc + sizeof(uint4) * kDescCap);
 constexpr size_t kScratchBytes = al256(kOffCheck + 256);
@@ -220,9 +219,9 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.ws.mid = const_cast<uint32_t *>(row_dev + 1);
     a.ws.ring = reinterpret_cast<uint32_t *>(b + kOffRing);
     a.ws.fq = reinterpret_cast<uint32_t *>(b + kOffFq);
-    a.ws.S = reinterpret_cast<uint32_t *>(b + kOffS);
     a.ws.pend = reinterpret_cast<uint32_t *>(b + kOffPend);
     a.ws.desc = reinterpret_cast<uint4 *>(b + kOffDesc);
+    a.ws.hdesc = nullptr;   // every edge is light here: no heavy descriptors
     a.ws.desc_cap = (uint32_t)kDescCap;
     a.ws.trace = nullptr;
     a.ws.trace_cap = 0;

@@ -50,21 +50,21 @@ __device__ __forceinline__ Exec cta_exec() {
 // ------------------------------------------------------------------- SCAN
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
-// A light scan relaxes the row prefix [row, mid), or the whole row when full;
-// a heavy scan the rest [mid, end).
+// The scan relaxes the light prefix [row, mid) of each row, or the whole row
+// when full.  With a split, a vertex scanned for the first time in the
+// current heavy round also emits descriptors for its heavy edges [mid, end):
+// the HEAVY phase relaxes them once the bucket's light loop has settled.
 template <int WT>
 __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x, const uint32_t *F,
-                              uint32_t count, uint32_t vtag, bool light, bool full, bool add_s, uint32_t hround,
-                              uint32_t &imp) {
+                              uint32_t count, uint32_t vtag, bool full, uint32_t hround, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
-    const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
     uint32_t my_edges = 0;
     uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
         const uint32_t i = base + lane;
-        uint32_t u = 0, s = 0, e = 0;
+        uint32_t u = 0, s = 0, e = 0, he = 0;
         typename Arith<WT>::D du = 0;
         bool ok = false;
         if (i < count) {
@@ -72,16 +72,18 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             // the tag check and the row reads are independent: issue together
             const uint32_t tg = (vtag == kTagInit) ? vtag : __ldcg(a.ws.tag + u);
             du = dist_of<WT>(__ldcg(a.ws.dp + u));
-            const uint32_t md = full ? __ldg(a.g.row + u + 1) : __ldg(a.ws.mid + u);
-            const uint32_t r = light ? __ldg(a.g.row + u) : __ldg(a.g.row + u + 1);
+            const uint32_t r = __ldg(a.g.row + u);
+            const uint32_t re = __ldg(a.g.row + u + 1);
+            const uint32_t md = full ? re : __ldg(a.ws.mid + u);
             ok = tg == vtag;
-            s = ok ? (light ? r : md) : 0u;
-            e = ok ? (light ? md : r) : 0u;
+            s = ok ? r : 0u;
+            e = ok ? md : 0u;
+            he = ok ? re : 0u;
         }
-        // S membership is decided now; the append waits until after the
-        // relaxation below so its latency overlaps that work
+        // heavy-round membership is decided now; the heavy descriptors are
+        // written after the relaxation below so this latency overlaps it
         uint32_t hold = hround;
-        if (ok && add_s) hold = atomicExch(a.ws.hst + u, hround);
+        if (ok && !full) hold = atomicExch(a.ws.hst + u, hround);
         const uint32_t len = e - s;
         // long rows -> descriptors, reserved with one atomic per warp
         const uint32_t nd = len > a.inline_max ? (len + kDescEdges - 1) / kDescEdges : 0u;
@@ -111,13 +113,105 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
         }
         // short rows: relaxed by this warp now
         relax_group<WT>(a, t, u, du, s, nd ? 0u : len, nc, imp);
-        warp_append(a.ws.S + (size_t)(hround & 1u) * n, &ctl->s_cnt[hround & 1u].v, n,
-                    ok && add_s && hold != hround, u, ctl);
+        if (!full) {
+            const uint32_t hlen = (ok && hold != hround) ? he - e : 0u;
+            const uint32_t hn = (hlen + kDescEdges - 1) / kDescEdges;
+            uint32_t hincl = hn;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, hincl, o);
+                if ((int)lane >= o) hincl += y;
+            }
+            const uint32_t htotal = __shfl_sync(FULL, hincl, 31);
+            if (htotal) {
+                uint32_t hbase = 0;
+                if (lane == 31) hbase = atomicAdd(&ctl->hdesc_cnt.v, htotal);
+                hbase = __shfl_sync(FULL, hbase, 31);
+                const uint32_t pos = hbase + hincl - hn;
+                if (pos + hn <= a.ws.desc_cap) {
+                    for (uint32_t c = 0; c < hn; ++c) {
+                        const uint32_t cs = e + c * kDescEdges;
+                        a.ws.hdesc[pos + c] = make_uint4(u, 0u, cs, min(he, cs + kDescEdges));
+                    }
+                } else if (hn) {
+                    atomicExch(&ctl->error, (uint32_t)kErrCapacity);
+                }
+            }
+        }
     }
     cand_drain<WT>(a, t, nc, imp);
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
     if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
+}
+
+// Warp-collective: relaxes one chunk [first, end) (<= kDescEdges edges) of
+// source u with all 32 lanes.
+template <int WT>
+__device__ __forceinline__ void relax_chunk(const SsspArgs &a, const Targets &t, uint32_t u,
+                                            typename Arith<WT>::D du, uint32_t first, uint32_t end, uint32_t &nc,
+                                            uint32_t &imp) {
+    const unsigned lane = lane_id();
+    uint32_t v[kUnroll], uo[kUnroll];
+    typename Arith<WT>::Wt w[kUnroll];
+    typename Arith<WT>::D duo[kUnroll];
+    bool val[kUnroll];
+#pragma unroll
+    for (int j = 0; j < kUnroll; ++j) {
+        const uint32_t e = first + 32u * j + lane;
+        val[j] = e < end;
+        uo[j] = u;
+        duo[j] = du;
+        v[j] = 0;
+        w[j] = 0;
+        if (val[j]) {
+            const uint2 ew = ld_stream(a.g.adj + e);
+            v[j] = ew.x;
+            w[j] = weight_at<WT>(a, e, ew);
+        }
+    }
+    relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
+}
+
+// ------------------------------------------------------------------ HEAVY
+// One thread per heavy descriptor, with dist(u) read from dp: u's distance
+// after the bucket's light loop.  Chunks longer than kInlineEdges are relaxed
+// one after another by the whole warp; the shorter ones (most heavy ranges of
+// a sparse graph) together, packed across the warp by a prefix sum.
+template <int WT>
+__device__ void relax_heavy(const SsspArgs &a, const Targets &t, const Exec &x, uint32_t count, uint32_t &imp) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    uint32_t nc = 0;   // candidates buffered by this warp
+    uint32_t my_edges = 0;
+    for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
+        const uint32_t i = base + lane;
+        uint32_t u = 0, s = 0, len = 0;
+        typename Arith<WT>::D du = 0;
+        if (i < count) {
+            const uint4 d = __ldcg(a.ws.hdesc + i);
+            u = d.x;
+            s = d.z;
+            len = d.w - d.z;
+            du = dist_of<WT>(__ldcg(a.ws.dp + u));
+        }
+        my_edges += len;
+        const bool lng = len > kInlineEdges;
+        unsigned lm = __ballot_sync(FULL, lng);
+        while (lm) {
+            const int src = __ffs(lm) - 1;
+            lm &= lm - 1u;
+            const uint32_t su = __shfl_sync(FULL, u, src);
+            const uint32_t ss = __shfl_sync(FULL, s, src);
+            const uint32_t sl = __shfl_sync(FULL, len, src);
+            const typename Arith<WT>::D sd = __shfl_sync(FULL, du, src);
+            relax_chunk<WT>(a, t, su, sd, ss, ss + sl, nc, imp);
+        }
+        relax_group<WT>(a, t, u, du, s, lng ? 0u : len, nc, imp);
+    }
+    cand_drain<WT>(a, t, nc, imp);
+    for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
+    if (lane == 0 && my_edges) atomicAdd(&a.ws.ctl->edge_cnt.v, my_edges);
 }
 
 // ------------------------------------------------------------------ EDGES
@@ -129,28 +223,11 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exe
     uint32_t nc = 0;   // candidates buffered by this warp
     for (uint32_t c = x.warp; c < count; c += x.nwarps) {
         const uint4 d = __ldcg(a.ws.desc + c);
+        // float64 distances do not fit the descriptor: read dp[u] again
         typename Arith<WT>::D du;
         if constexpr (WT == kWF64) du = dist_of<WT>(__ldcg(a.ws.dp + d.x));
         else du = d.y;
-        uint32_t v[kUnroll], uo[kUnroll];
-        typename Arith<WT>::Wt w[kUnroll];
-        typename Arith<WT>::D duo[kUnroll];
-        bool val[kUnroll];
-#pragma unroll
-        for (int j = 0; j < kUnroll; ++j) {
-            const uint32_t e = d.z + 32u * j + lane;
-            val[j] = e < d.w;
-            uo[j] = d.x;
-            duo[j] = du;
-            v[j] = 0;
-            w[j] = 0;
-            if (val[j]) {
-                const uint2 ew = ld_stream(a.g.adj + e);
-                v[j] = ew.x;
-                w[j] = weight_at<WT>(a, e, ew);
-            }
-        }
-        relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
+        relax_chunk<WT>(a, t, d.x, du, d.z, d.w, nc, imp);
     }
     cand_drain<WT>(a, t, nc, imp);
 }
@@ -270,19 +347,15 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
             for (uint32_t j = 0; j < U.span; ++j) {
                 const uint32_t bk = U.b + j;
                 scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n,
-                                   min(__ldcg(&ctl->ring_cnt[bk % kNB].v), n), bk, true, full, !full, U.hround,
-                                   imp);
+                                  min(__ldcg(&ctl->ring_cnt[bk % kNB].v), n), bk, full, U.hround, imp);
             }
             break;
         case kPhLight:
             scan_frontier<WT>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                               min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, true, full, !full,
-                               U.hround, imp);
+                              min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, full, U.hround, imp);
             break;
         case kPhHeavy:
-            scan_frontier<WT>(a, t, x, a.ws.S + (size_t)(U.hround & 1u) * n,
-                               min(__ldcg(&ctl->s_cnt[U.hround & 1u].v), n), kTagInit, false, false, false,
-                               U.hround, imp);
+            relax_heavy<WT>(a, t, x, min(__ldcg(&ctl->hdesc_cnt.v), a.ws.desc_cap), imp);
             break;
         case kPhEdges:
             relax_descriptors<WT>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
@@ -467,7 +540,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     const uint32_t edge_cnt = ld_relaxed(&ctl->edge_cnt.v);
     const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u].v);
     const uint32_t fq_cur = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u].v);
-    const uint32_t s_cur = ld_relaxed(&ctl->s_cnt[U.hround & 1u].v);
+    const uint32_t hd_cnt = ld_relaxed(&ctl->hdesc_cnt.v);
     const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0].v), pc1 = ld_relaxed(&ctl->pend_cnt[1].v);
     const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0].v), pm1 = ld_relaxed(&ctl->pend_min[1].v);
     const uint32_t err = ld_relaxed(&ctl->error);
@@ -509,7 +582,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         const uint32_t logical = (U.phase == kPhEdges) ? U.logical : scan_kind(U.phase);
         if (fq_next > 0) {
             next = kPhLight;
-        } else if (logical == kPhLight && !U.full) {
+        } else if (logical == kPhLight && !U.full && hd_cnt > 0) {
             next = kPhHeavy;
         } else {
             bucket_end = true;
@@ -583,7 +656,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     switch (next) {
         case kPhLightFirst: items = first_items; break;
         case kPhLight: items = fq_next; break;
-        case kPhHeavy: items = s_cur; break;
+        case kPhHeavy: items = hd_cnt; break;
         case kPhEdges: items = desc_cnt; break;
         case kPhPending: items = ps2 ? pc1 : pc0; break;
         default: break;
@@ -601,7 +674,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
                 switch (U.phase) {
                     case kPhLightFirst: done_items = cur_ring; break;
                     case kPhLight: done_items = fq_cur; break;
-                    case kPhHeavy: done_items = s_cur; break;
+                    case kPhHeavy: done_items = hd_cnt; break;
                     case kPhEdges: done_items = desc_cnt; break;
                     default: done_items = U.pend_sel ? pc1 : pc0; break;
                 }
@@ -647,7 +720,9 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             ctl->fq_cnt[(N.epoch + 1u) % 3u].v = 0;
             ctl->desc_cnt.v = 0;
             ctl->edge_cnt.v = 0;
-            if (N.hround != U.hround || next == kPhLightFirst) ctl->s_cnt[N.hround & 1u].v = 0;
+            // heavy descriptors of the next heavy round start over once the
+            // last round's are relaxed, and at every new bucket
+            if (U.phase == kPhHeavy || next == kPhLightFirst) ctl->hdesc_cnt.v = 0;
         }
         ctl->pub_phase = N.phase;
         ctl->pub_logical = N.logical;
@@ -675,7 +750,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             a.ws.ring[0] = a.inst[inst].source;
             for (int i = 0; i < 3; ++i) ctl->fq_cnt[i].v = 0u;
             for (int i = 0; i < 2; ++i) {
-                ctl->s_cnt[i].v = 0u;
+                ctl->hdesc_cnt.v = 0u;
                 ctl->pend_cnt[i].v = 0u;
                 ctl->pend_min[i].v = kTagInit;
             }

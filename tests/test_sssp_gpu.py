@@ -151,7 +151,7 @@ def test_split_covering_all_edges_skips_heavy(wtype, gb, orc):
         for light, heavy_expected in [(wmax, False), (wmax * 4, False), (wmax - 1, True)]:
             d, p, st = g.sssp(src, delta=wmax / 8, light=light, flags=gb.F_TRACE)
             kinds = {r["kind"] for r in g.trace()}
-            assert ("scan_heavy" in kinds) == heavy_expected, (light, kinds)
+            assert ("heavy" in kinds) == heavy_expected, (light, kinds)
             ref = orc.dijkstra(a.row, a.col, a.w, src)
             assert np.array_equal(d, ref)
             assert np.array_equal(p, orc.min_tight_pred(a.row, a.col, a.w, src, ref))
