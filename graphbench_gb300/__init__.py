@@ -35,7 +35,7 @@ F_NO_STATS = 0x1
 EXPORTS = [
     "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
-    "gbs_sssp_multi", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
+    "gbs_sssp_multi", "gbs_bc", "gbs_bc_device", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
     "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
     "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
     "gbs_autotune", "gbs_autotune_plan_sources", "gbs_autotune_plan_pack",
@@ -90,6 +90,16 @@ class Stats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BcStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("sssp_ms", ctypes.c_double), ("dag_ms", ctypes.c_double),
+                ("edges_reached", ctypes.c_uint64), ("tight_edges", ctypes.c_uint64),
+                ("dag_vertices", ctypes.c_uint64), ("max_levels", ctypes.c_uint32),
+                ("sources", ctypes.c_uint32), ("blocks", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class CsrView(ctypes.Structure):
@@ -160,6 +170,8 @@ def _load() -> ctypes.CDLL:
                                   ctypes.POINTER(Stats)]
     L.gbs_sssp_multi.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, P,
                                  ctypes.POINTER(Stats)]
+    L.gbs_bc.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
+    L.gbs_bc_device.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
     L.gbs_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
     L.gbs_host_free.argtypes = [P]
     L.gbs_device_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
@@ -469,6 +481,31 @@ class Graph:
         r = {k: getattr(rep, k) for k, _ in TuneReport._fields_ if k != "best"}
         r["best"] = dict(kw)
         return kw, r
+
+    def betweenness(self, sources=None, delta: float | None = None, light: float | None = None,
+                    out: np.ndarray | None = None, **kw):
+        """Betweenness centrality summed over `sources` (every vertex when
+        None), as run_bc computes it (btwcentral/csr_bc.c:16-64).  Returns
+        (bc float64[n], stats dict)."""
+        p = self.params(delta, light, **kw)
+        st = BcStats()
+        bc = out if out is not None else np.empty(self.n, dtype=np.float64)
+        src = None if sources is None else np.ascontiguousarray(sources, dtype=np.uint32)
+        _check(lib.gbs_bc(self._h, _ptr(src) if src is not None else None,
+                          len(src) if src is not None else 0, ctypes.byref(p), _ptr(bc),
+                          ctypes.byref(st)), "gbs_bc")
+        return bc, st.as_dict()
+
+    def betweenness_device(self, bc_ptr: int, sources=None, delta: float | None = None,
+                           light: float | None = None, **kw) -> dict:
+        """Betweenness into caller-owned device memory (n doubles)."""
+        p = self.params(delta, light, **kw)
+        st = BcStats()
+        src = None if sources is None else np.ascontiguousarray(sources, dtype=np.uint32)
+        _check(lib.gbs_bc_device(self._h, _ptr(src) if src is not None else None,
+                                 len(src) if src is not None else 0, ctypes.byref(p), bc_ptr,
+                                 ctypes.byref(st)), "gbs_bc_device")
+        return st.as_dict()
 
     def sssp_multi(self, sources, delta: float | None = None, light: float | None = None,
                    want_dist: bool = True, want_pred: bool = False, **kw):

@@ -349,6 +349,7 @@ void free_graph(gbs_graph *g) {
     cudaFree(g->d_pred);
     cudaFree(g->d_mlp);
     cudaFree(g->d_feat);
+    free_bc(g);
     for (auto &e : g->ev) if (e) cudaEventDestroy(e);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
@@ -744,6 +745,10 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
     g->wtype = wtype;
     g->max_w = max_w;
     g->mean_w = m ? wsum / (double)m : 0.0;
+    // rows are sorted by weight: a zero weight is the first of its row
+    for (uint32_t v = 0; v < n && !g->zero_w; ++v)
+        if (row32[v] < row32[v + 1])
+            g->zero_w = wtype == GBS_WEIGHT_F64 ? w64[row32[v]] == 0ull : adj[row32[v]].y == 0u;
     g->device = dev;
     cudaError_t e;
     if ((e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||

@@ -33,6 +33,7 @@ struct gbs_graph {
     uint64_t m = 0;
     gbs_weight_type wtype = GBS_WEIGHT_U32;
     double max_w = 0.0;
+    bool zero_w = false;                    // some edge weighs 0
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
@@ -61,6 +62,8 @@ struct gbs_graph {
     // recorded controller inputs (GBS_F_FEATURES)
     float *d_feat = nullptr;
     uint32_t feat_cap = 0, feat_n = 0;
+    // betweenness state (gbs_bc), allocated on first use
+    void *bc = nullptr;
 };
 
 namespace gbs {
@@ -109,5 +112,15 @@ void free_workspace(Workspace &w);
 
 // Resident CTAs of the persistent kernels on one SM (0 if they cannot run).
 int persistent_ctas_per_sm(gbs_weight_type wt, bool batch);
+
+// Allocates the single-source workspace of a graph on first use.
+gbs_status ensure_workspace(gbs_graph *g);
+// One single-source run (learned controller and its guard included) with the
+// outputs in device memory (either may be null); the distances stay in the
+// workspace's state words until the next run.
+gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_dev, int32_t *pred_dev,
+                    gbs_stats *stats);
+// Releases the betweenness state of a graph.
+void free_bc(gbs_graph *g);
 
 }  // namespace gbs

@@ -168,6 +168,42 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
                           gbs_stats *stats);
 
 /*
+ * Betweenness centrality (Brandes over shortest paths), the computation of
+ * run_bc (btwcentral/csr_bc.c:16-64) on a resident graph instead of a file:
+ * for every source s (sources[0..k), or every vertex when sources is NULL)
+ * bc[v] += delta_s(v) for v != s, where delta_s(v) = sum over the tight
+ * out-edges (v, w) -- dist(v) + w == dist(w) in the weight type -- of
+ * (1 + delta_s(w)) * sigma_s(v) / sigma_s(w), and sigma_s counts the tight
+ * paths from s (comp_num_spath / comp_delta, csr_bc.c:67-116; sigma in
+ * 64-bit integers like the reference's lint, the rest in double).  Each
+ * tight edge is counted once (the reference's predecessor lists can hold an
+ * entry more than once, sssp/csr_sspath.c:100-118, which changes its result
+ * when a vertex has several shortest-path predecessors).  Weights must be
+ * positive (GBS_ERR_INVALID_ARG otherwise).  bc_out: n doubles in host
+ * memory.  params: the schedule of the shortest-path runs (NULL: the
+ * default); the result does not depend on it.
+ */
+typedef struct gbs_bc_stats {
+    double device_ms;        /* CUDA-event time of all shortest-path runs and DAG passes */
+    double sssp_ms;          /* the shortest-path runs alone */
+    double dag_ms;           /* the path-count / dependency passes alone */
+    uint64_t edges_reached;  /* sum over sources of the edges out of reached vertices */
+    uint64_t tight_edges;    /* sum over sources of the shortest-path DAG's edges */
+    uint64_t dag_vertices;   /* sum over sources of the reached vertices */
+    uint32_t max_levels;     /* deepest DAG in hop levels (the source's is level 0) */
+    uint32_t sources;
+    uint32_t blocks;         /* CTAs of the DAG kernel */
+    uint32_t reserved;
+} gbs_bc_stats;
+
+gbs_status gbs_bc(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_params *params,
+                  double *bc_out, gbs_bc_stats *stats);
+
+/* Same with the result in DEVICE memory (n doubles, cudaMalloc). */
+gbs_status gbs_bc_device(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_params *params,
+                         double *bc_dev, gbs_bc_stats *stats);
+
+/*
  * Per-phase record of the last run made with GBS_F_TRACE (the GPU analogue
  * of the reference's per-phase rdtsc slots and bucket dumps,
  * sssp/csr_sspath_array.c:1121-1170).  kind (low 4 bits; +16 if the phase ran

@@ -66,6 +66,9 @@ def lib() -> ctypes.CDLL:
         for name in ("or_delta_stepping_u32", "or_delta_stepping_f32", "or_delta_stepping_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _dbl, _P, _P]
             getattr(L, name).restype = ctypes.c_int
+        for name in ("or_bc_u32", "or_bc_f32", "or_bc_f64"):
+            getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _P, _P]
+            getattr(L, name).restype = ctypes.c_int
         L.or_count_tight_preds_f64.argtypes = [_u32, _P, _P, _P, _u32, _P, _P]
         L.or_fill_tight_preds_f64.argtypes = [_u32, _P, _P, _P, _u32, _P, _P, _P, _P]
         _lib = L
@@ -193,6 +196,8 @@ def ref_lib(variant: str = "serial") -> ctypes.CDLL:
         L.gbref_sssp_arr.restype = ctypes.c_int
         L.gbref_sssp_list.argtypes = [_i64, _i64, _P, _P, _P, _i64, _dbl, _P, _P, _P, _i64, _P]
         L.gbref_sssp_list.restype = ctypes.c_int
+        L.gbref_bc.argtypes = [_i64, _i64, _P, _P, _P, _i64, _P, _dbl, ctypes.c_int, _P, _P, _P]
+        L.gbref_bc.restype = ctypes.c_int
         _ref_libs[variant] = L
     return _ref_libs[variant]
 
@@ -248,3 +253,45 @@ def ref_sssp_list(row, col, w, src: int, delta: float, pred_cap: int | None = No
     if rc != 0:
         raise RuntimeError(f"reference run_sspath failed (code {rc})")
     return dist, cnt, lst[: int(cnt.sum())], float(secs[0])
+
+
+def ref_bc(row, col, w, sources=None, delta: float = 0.1, dedup: bool = False):
+    """The reference's Brandes loop (btwcentral/csr_bc.c:40-59: run_sspath,
+    q_sort_double, comp_num_spath, comp_delta) on this CSR.  Returns
+    (bc float64[n], duplicated predecessor entries, seconds).  run_sspath
+    allocates 1000 buckets, so every distance must stay below 1000 * delta.
+    ``dedup`` drops repeated entries of each predecessor list before the
+    path counts (run_sspath appends a predecessor again whenever it
+    re-relaxes an edge to an equal distance)."""
+    row64 = np.ascontiguousarray(row, dtype=np.int64)
+    col64 = np.ascontiguousarray(col, dtype=np.int64)
+    wd = np.ascontiguousarray(w, dtype=np.float64)
+    n = len(row64) - 1
+    src = None if sources is None else np.ascontiguousarray(sources, dtype=np.int64)
+    k = n if src is None else len(src)
+    bc = np.empty(n, dtype=np.float64)
+    dups = np.zeros(1, dtype=np.int64)
+    secs = np.zeros(1, dtype=np.float64)
+    rc = ref_lib("serial").gbref_bc(n, int(row64[-1]), _ptr(row64), _ptr(col64), _ptr(wd), k,
+                                    _ptr(src) if src is not None else None, float(delta),
+                                    int(bool(dedup)), _ptr(bc), _ptr(dups), _ptr(secs))
+    if rc != 0:
+        raise RuntimeError(f"reference BC failed (code {rc})")
+    return bc, int(dups[0]), float(secs[0])
+
+
+def betweenness(row, col, w, sources=None) -> np.ndarray:
+    """Brandes betweenness over shortest paths summed over `sources` (all
+    vertices when None), restating btwcentral/csr_bc.c:16-123 with each tight
+    predecessor counted once.  Weights must be positive."""
+    row, col, w = _prep(row, col, w)
+    n = len(row) - 1
+    bc = np.zeros(n, dtype=np.float64)
+    src = None if sources is None else np.ascontiguousarray(sources, dtype=np.uint32)
+    k = n if src is None else len(src)
+    fn = {np.dtype(np.uint32): lib().or_bc_u32, np.dtype(np.float32): lib().or_bc_f32,
+          np.dtype(np.float64): lib().or_bc_f64}[w.dtype]
+    rc = fn(n, _ptr(row), _ptr(col), _ptr(w), k, _ptr(src) if src is not None else None, _ptr(bc))
+    if rc != 0:
+        raise RuntimeError(f"oracle betweenness failed ({rc})")
+    return bc

@@ -479,3 +479,99 @@ int or_delta_stepping_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
                           double *d, int64_t *phases) {
     OR_DS_BODY(double, double)
 }
+
+/* ------------------------------------------------ betweenness centrality */
+/* Brandes over shortest paths, after btwcentral/csr_bc.c:16-123: for every
+ * source, vertices in increasing distance order (csr_bc.c:43-49, q_sort of
+ * the distances; ties broken by vertex id here), path counts
+ * sigma[w] = sum of sigma over the tight predecessors of w (comp_num_spath,
+ * :69-91), dependencies in decreasing order
+ * delta[v] += (1 + delta[w]) * sigma[v] / sigma[w] for every tight
+ * predecessor v != source of w (comp_delta, :93-116), and bc[v] += delta[v]
+ * for v != source (:54-58).  The predecessors are the tight in-edges, each
+ * once (the reference's list path can hold one twice).  Path counts are
+ * 64-bit sums that wrap like the reference's lint.  Weights must be positive
+ * so that a predecessor's distance is strictly smaller. */
+typedef struct { double d; uint32_t v; } or_dv;
+static int cmp_dv(const void *a, const void *b) {
+    const or_dv *x = (const or_dv *)a, *y = (const or_dv *)b;
+    if (x->d < y->d) return -1;
+    if (x->d > y->d) return 1;
+    return (x->v > y->v) - (x->v < y->v);
+}
+
+#define OR_BC_BODY(DT, WT, DIJKSTRA, TIGHT, INF_TEST)                                     \
+    uint64_t *rrow = (uint64_t *)calloc((size_t)n + 1, 8);                                \
+    uint32_t *rsrc = (uint32_t *)malloc(sizeof(uint32_t) * (row[n] ? row[n] : 1));        \
+    WT *rw = (WT *)malloc(sizeof(WT) * (row[n] ? row[n] : 1));                            \
+    DT *dist = (DT *)malloc(sizeof(DT) * n);                                              \
+    uint64_t *sig = (uint64_t *)malloc(8 * (size_t)n);                                    \
+    double *del = (double *)malloc(8 * (size_t)n);                                        \
+    or_dv *ord = (or_dv *)malloc(sizeof(or_dv) * n);                                      \
+    uint64_t *cur = (uint64_t *)malloc(8 * ((size_t)n + 1));                              \
+    int rc = 0;                                                                           \
+    if (!rrow || !rsrc || !rw || !dist || !sig || !del || !ord || !cur) rc = -1;          \
+    for (uint32_t v = 0; v < n && !rc; v++) bc[v] = 0.0;                                  \
+    /* in-edges (transpose) */                                                            \
+    for (uint32_t u = 0; u < n && !rc; u++)                                               \
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) rrow[col[e] + 1]++;                \
+    for (uint32_t v = 0; v < n && !rc; v++) rrow[v + 1] += rrow[v];                       \
+    for (uint32_t v = 0; v <= n && !rc; v++) cur[v] = rrow[v];                            \
+    for (uint32_t u = 0; u < n && !rc; u++)                                               \
+        for (uint64_t e = row[u]; e < row[u + 1]; e++) {                                  \
+            uint64_t p = cur[col[e]]++;                                                   \
+            rsrc[p] = u;                                                                  \
+            rw[p] = w[e];                                                                 \
+        }                                                                                 \
+    for (uint32_t k = 0; k < nsrc && !rc; k++) {                                          \
+        const uint32_t s = srcs ? srcs[k] : k;                                            \
+        if (DIJKSTRA(n, row, col, w, s, dist)) { rc = -1; break; }                        \
+        for (uint32_t v = 0; v < n; v++) {                                                \
+            ord[v].d = INF_TEST(dist[v]) ? INFINITY : (double)dist[v];                    \
+            ord[v].v = v;                                                                 \
+            sig[v] = 0;                                                                   \
+            del[v] = 0.0;                                                                 \
+        }                                                                                 \
+        qsort(ord, n, sizeof(or_dv), cmp_dv);                                             \
+        sig[s] = 1;                                                                       \
+        for (uint32_t i = 0; i < n; i++) {                                                \
+            const uint32_t x = ord[i].v;                                                  \
+            if (x == s || INF_TEST(dist[x])) continue;                                    \
+            for (uint64_t e = rrow[x]; e < rrow[x + 1]; e++) {                            \
+                const uint32_t v = rsrc[e];                                               \
+                if (!INF_TEST(dist[v]) && TIGHT(dist[v], rw[e], dist[x])) sig[x] += sig[v]; \
+            }                                                                             \
+        }                                                                                 \
+        for (uint32_t i = n; i-- > 0;) {                                                  \
+            const uint32_t x = ord[i].v;                                                  \
+            if (x == s || INF_TEST(dist[x])) continue;                                    \
+            for (uint64_t e = rrow[x]; e < rrow[x + 1]; e++) {                            \
+                const uint32_t v = rsrc[e];                                               \
+                if (v != s && !INF_TEST(dist[v]) && TIGHT(dist[v], rw[e], dist[x]))       \
+                    del[v] += (1.0 + del[x]) * (double)(int64_t)sig[v] / (double)(int64_t)sig[x]; \
+            }                                                                             \
+        }                                                                                 \
+        for (uint32_t v = 0; v < n; v++)                                                  \
+            if (v != s) bc[v] += del[v];                                                  \
+    }                                                                                     \
+    free(rrow); free(rsrc); free(rw); free(dist); free(sig); free(del); free(ord); free(cur); \
+    return rc;
+
+#define OR_TIGHT_U32(du, w, dv) ((uint64_t)(du) + (w) == (uint64_t)(dv))
+#define OR_INF_U32(d) ((d) == OR_UNREACHED_U32)
+static int or_tight_f32(float du, float w, float dv) { volatile float s = du + w; return s == dv; }
+static int or_tight_f64(double du, double w, double dv) { volatile double s = du + w; return s == dv; }
+#define OR_INF_FP(d) (isinf(d))
+
+int or_bc_u32(uint32_t n, const uint64_t *row, const uint32_t *col, const uint32_t *w, uint32_t nsrc,
+              const uint32_t *srcs, double *bc) {
+    OR_BC_BODY(uint32_t, uint32_t, or_dijkstra_u32, OR_TIGHT_U32, OR_INF_U32)
+}
+int or_bc_f32(uint32_t n, const uint64_t *row, const uint32_t *col, const float *w, uint32_t nsrc,
+              const uint32_t *srcs, double *bc) {
+    OR_BC_BODY(float, float, or_dijkstra_f32, or_tight_f32, OR_INF_FP)
+}
+int or_bc_f64(uint32_t n, const uint64_t *row, const uint32_t *col, const double *w, uint32_t nsrc,
+              const uint32_t *srcs, double *bc) {
+    OR_BC_BODY(double, double, or_dijkstra_f64, or_tight_f64, OR_INF_FP)
+}

@@ -226,3 +226,99 @@ int gbref_sssp_list(int64_t n, int64_t m, const int64_t *row, const int64_t *col
     munmap(map, map_bytes);
     return rc;
 }
+
+/* btwcentral/csr_bc.c:16-64 (run_bc) without its file reading: for every
+ * source in `srcs` (all vertices when srcs is NULL) run_sspath with bucket
+ * width `delta` (run_bc passes 0.1), sort the distances with q_sort_double
+ * (utils/utils.c:82), then the reference's comp_num_spath and comp_delta
+ * (csr_bc.c:67-116), summing delta[j] over j != source into bc_out.  Runs in
+ * one forked child; dup_out (may be NULL) receives how many predecessor list
+ * entries repeated an earlier entry of the same list, summed over sources.
+ * With `dedup` set, such repeats are unlinked before comp_num_spath runs
+ * (run_sspath appends u again each time it re-relaxes an edge to an equal
+ * distance, sssp/csr_sspath.c:100-118, and its S list is never emptied,
+ * :51-72, so heavy edges are re-relaxed every bucket). */
+void q_sort_double(double *a, lint *b, lint l, lint r);
+void comp_num_spath(lint source, lint *num_spath, lint *dis_idx, p_list *predecesor, lint v_size);
+void comp_delta(lint source, lint *num_spath, double *delta, lint *dis_idx, p_list *predecesor,
+                lint v_size);
+void empty_predecesor(p_list *predecesor, lint v_size);
+
+int gbref_bc(int64_t n, int64_t m, const int64_t *row, const int64_t *col, const double *w,
+             int64_t nsrc, const int64_t *srcs, double delta, int dedup, double *bc_out,
+             int64_t *dup_out, double *seconds) {
+    size_t map_bytes = sizeof(ref_result) + sizeof(double) * (size_t)(n ? n : 1);
+    void *map = mmap(NULL, map_bytes, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
+    if (map == MAP_FAILED) return -10;
+    ref_result *res = (ref_result *)map;
+    double *tot = (double *)((char *)map + sizeof(ref_result));
+    res->status = -1;
+    fflush(NULL);
+    pid_t pid = fork();
+    if (pid < 0) { munmap(map, map_bytes); return -11; }
+    if (pid == 0) {
+        char dir[64];
+        if (enter_scratch(dir, sizeof dir) != 0) _exit(3);
+        quiet_stdout();
+        t_csr *gs = make_csr(n, m, row, col, w);
+        p_list *pred = (p_list *)malloc(sizeof(p_list) * (n ? n : 1));
+        double *dl = (double *)malloc(sizeof(double) * (n ? n : 1));
+        double *distance = (double *)malloc(sizeof(double) * (n ? n : 1));
+        lint *dis_idx = (lint *)malloc(sizeof(lint) * (n ? n : 1));
+        lint *num_spath = (lint *)malloc(sizeof(lint) * (n ? n : 1));
+        unsigned char *seen = (unsigned char *)calloc((size_t)(n ? n : 1), 1);
+        for (int64_t v = 0; v < n; v++) {
+            pred[v] = (p_list)malloc(sizeof(t_list));
+            creat_list(pred[v]);
+            tot[v] = 0.0;
+        }
+        int64_t dups = 0;
+        double t0 = now_s();
+        for (int64_t k = 0; k < nsrc; k++) {
+            lint source = srcs ? srcs[k] : k;
+            run_sspath(gs, pred, source, delta);
+            for (int64_t j = 0; j < n; j++) {
+                distance[j] = gs->vet_info[j].weight;
+                dis_idx[j] = j;
+            }
+            q_sort_double(distance, dis_idx, 0, n - 1);
+            for (int64_t v = 0; v < n; v++) {
+                for (p_list q = pred[v], p = q->next; p; p = q->next) {
+                    if (seen[p->int_val]) {
+                        dups++;
+                        if (dedup) { q->next = p->next; free(p); continue; }
+                    }
+                    seen[p->int_val] = 1;
+                    q = p;
+                }
+                for (p_list p = pred[v]->next; p; p = p->next) seen[p->int_val] = 0;
+            }
+            comp_num_spath(source, num_spath, dis_idx, pred, n);
+            comp_delta(source, num_spath, dl, dis_idx, pred, n);
+            for (int64_t j = 0; j < n; j++)
+                if (j != source) tot[j] += dl[j];
+            empty_predecesor(pred, n);
+        }
+        double t1 = now_s();
+        res->pred_total = dups;
+        res->seconds = t1 - t0;
+        res->status = 0;
+        unlink("data/log/ori");
+        rmdir("data/log");
+        rmdir("data");
+        if (chdir("/tmp") == 0) rmdir(dir);
+        _exit(0);
+    }
+    int st = 0;
+    waitpid(pid, &st, 0);
+    int rc = 0;
+    if (!WIFEXITED(st) || WEXITSTATUS(st) != 0 || res->status != 0) {
+        rc = WIFSIGNALED(st) ? -100 - WTERMSIG(st) : -12;
+    } else {
+        memcpy(bc_out, tot, sizeof(double) * (size_t)n);
+        if (dup_out) *dup_out = res->pred_total;
+        if (seconds) *seconds = res->seconds;
+    }
+    munmap(map, map_bytes);
+    return rc;
+}

@@ -16,6 +16,13 @@ Run from the repository root where the reference tree is present:
    result within float32 rounding (float32).
 3. ``rmat10_dist.npy`` / ``rmat10_pred.npy``: the full arrays of the first
    seeded case, for diagnostics.
+4. ``bc_golden.json``: betweenness centrality over every source of small
+   graphs, computed by the reference's own Brandes loop (run_sspath,
+   q_sort_double, comp_num_spath, comp_delta; btwcentral/csr_bc.c:40-59).
+   Where a vertex has several shortest-path predecessors the reference's
+   lists repeat entries unevenly, so those cases are recorded from the
+   reference with each list deduplicated (``dedup``); every case is checked
+   against the oracle's Brandes restatement before it is written.
 """
 from __future__ import annotations
 
@@ -204,15 +211,78 @@ def check_seeded(have_ref: bool):
     return out
 
 
+# (name, graph, dedup): u32 cases with small weight ranges have many equal
+# shortest paths (sigma > 1); the float64 case has fractional weights and
+# unique predecessors, where the reference's raw lists give Brandes' result.
+BC_CASES = [
+    dict(name="bc_path5", kind="known", known="path"),
+    dict(name="bc_diamond", kind="known", known="diamond_ties"),
+    dict(name="bc_star", kind="known", known="star"),
+    dict(name="bc_disconnected", kind="known", known="disconnected"),
+    dict(name="bc_parallel", kind="known", known="parallel_edges"),
+    dict(name="bc_rmat7_w1_4", kind="rmat", scale=7, edgefactor=8, seed=3, wtype="u32", wmax=4),
+    dict(name="bc_rmat8_w1_255", kind="rmat", scale=8, edgefactor=8, seed=4, wtype="u32", wmax=255),
+    dict(name="bc_grid8x9_w1_2", kind="grid", rows=8, cols=9, seed=5, wtype="u32", wmax=2),
+    dict(name="bc_rmat7_f64", kind="rmat_f64", scale=7, edgefactor=8, seed=6),
+]
+
+
+def bc_graph(case):
+    if case["kind"] == "known":
+        kc = next(k for k in KNOWN if k["name"] == case["known"])
+        return to_csr(kc)
+    if case["kind"] == "rmat":
+        return gen.rmat(case["scale"], case["edgefactor"], case["seed"], "u32", 1, case["wmax"])
+    if case["kind"] == "grid":
+        return gen.grid(case["rows"], case["cols"], case["seed"], "u32", 1, case["wmax"])
+    row, col, w = gen.rmat(case["scale"], case["edgefactor"], case["seed"], "u32", 1, 255)
+    return row, col, col.astype(np.float64) / 384.0 + w.astype(np.float64) / 131.0
+
+
+def check_bc(have_ref: bool):
+    out = []
+    for case in BC_CASES:
+        row, col, w = bc_graph(case)
+        if np.asarray(w).dtype == np.float64:
+            w = np.asarray(w, dtype=np.float64)
+        bc = oracle.betweenness(row, col, w)
+        rec = dict(case)
+        rec.update(n=int(len(row) - 1), m=int(row[-1]), row_sha=sha(row), col_sha=sha(col), w_sha=sha(w))
+        if have_ref:
+            maxd = 0.0
+            for s in range(len(row) - 1):
+                d = oracle.dijkstra(row, col, w, s).astype(np.float64)
+                if np.asarray(w).dtype == np.uint32:
+                    d[d == float(U32MAX)] = np.inf
+                fin = d[np.isfinite(d)]
+                maxd = max(maxd, float(fin.max()) if len(fin) else 0.0)
+            delta = max(0.1, maxd / 900.0)
+            dedup = np.asarray(w).dtype != np.float64
+            ref, dups, _ = oracle.ref_bc(row, col, w, delta=delta, dedup=dedup)
+            rel = float(np.max(np.abs(ref - bc) / np.maximum(1.0, np.abs(ref))))
+            assert rel < 1e-12, (case["name"], rel)
+            rec.update(reference_delta=delta, reference_dedup=bool(dedup), reference_repeats=dups,
+                       max_rel_vs_oracle=rel)
+            rec["bc"] = [float(x) for x in ref]
+        else:
+            rec["bc"] = [float(x) for x in bc]
+        rec["from_reference"] = bool(have_ref)
+        out.append(rec)
+    return out
+
+
 def main():
     have_ref = build_ref.stage()
     if have_ref:
         build_ref.compile_ref()
     known = check_known(have_ref)
     seeded = check_seeded(have_ref)
+    bc = check_bc(have_ref)
+    (HERE / "bc_golden.json").write_text(json.dumps(bc) + "\n")
     (HERE / "known_answer.json").write_text(json.dumps(known, indent=1) + "\n")
     (HERE / "seeded.json").write_text(json.dumps(seeded, indent=1) + "\n")
-    print(f"wrote {len(known)} known-answer and {len(seeded)} seeded cases; reference checked: {have_ref}")
+    print(f"wrote {len(known)} known-answer, {len(seeded)} seeded and {len(bc)} betweenness cases; "
+          f"reference checked: {have_ref}")
 
 
 if __name__ == "__main__":
