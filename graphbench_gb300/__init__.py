@@ -68,7 +68,8 @@ class PhaseRec(ctypes.Structure):
                 ("end_ns", ctypes.c_uint64)]
 
 
-PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "heavy", 3: "relax", 4: "pending"}
+PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "heavy", 3: "relax", 4: "pending",
+               8: "bc_count", 9: "bc_forward", 10: "bc_backward", 11: "bc_backward_words"}
 F_TRACE = 0x2
 F_NO_SOLO = 0x4
 F_FEATURES = 0x8

@@ -213,6 +213,11 @@ gbs_status gbs_bc_device(gbs_graph *g, const uint32_t *sources, uint32_t k, cons
  * that had already left the pending list).  items: frontier entries
  * (scans), edge descriptors (relaxation) or pending entries; edges: edges
  * the scan handed to the relaxation; end_ns: device time since kernel start.
+ * After gbs_bc with GBS_F_TRACE the records are those of the last source's
+ * path-count / dependency launch: kind 8 the tight-edge count, 9 a forward
+ * level, 10 a backward level, 11 the first part of a backward level whose
+ * long rows are then finished; bucket = the level, items = its vertices,
+ * edges = the mask words of its rows longer than 32 edges.
  * *count receives the number of records (may exceed cap).
  */
 typedef struct gbs_phase_rec {

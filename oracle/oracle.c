@@ -485,13 +485,25 @@ int or_delta_stepping_f64(uint32_t n, const uint64_t *row, const uint32_t *col,
  * source, vertices in increasing distance order (csr_bc.c:43-49, q_sort of
  * the distances; ties broken by vertex id here), path counts
  * sigma[w] = sum of sigma over the tight predecessors of w (comp_num_spath,
- * :69-91), dependencies in decreasing order
- * delta[v] += (1 + delta[w]) * sigma[v] / sigma[w] for every tight
- * predecessor v != source of w (comp_delta, :93-116), and bc[v] += delta[v]
- * for v != source (:54-58).  The predecessors are the tight in-edges, each
- * once (the reference's list path can hold one twice).  Path counts are
- * 64-bit sums that wrap like the reference's lint.  Weights must be positive
- * so that a predecessor's distance is strictly smaller. */
+ * :69-91), then in decreasing order the dependencies
+ * delta[v] = sum over tight out-edges (v, w) of (1 + delta[w]) * sigma[v] /
+ * sigma[w] (comp_delta, :93-116, each term with its order of operations), and
+ * bc[v] += delta[v] for v != source (:54-58).  The tight edges are counted
+ * once each (the reference's list path can hold a predecessor twice).  Path
+ * counts are 64-bit sums that wrap like the reference's lint.  Weights must be
+ * positive so that a predecessor's distance is strictly smaller.
+ *
+ * Summation order of delta[v] (floating point, so it is fixed here): the row
+ * of v sorted by (weight, column) keeps its CSR positions row[v] ..
+ * row[v+1]-1, grouped in 32-position words (position / 32).  A word's sum is
+ * the butterfly of its 32 slots (slot = position % 32; 0 for positions of
+ * other rows and for edges that are not tight): for h = 16, 8, 4, 2, 1,
+ * s[i] = s[i] + s[i + h] for i < h, giving s[0].  The row's words, numbered
+ * from its first word, form blocks of 32; each block's word sums are combined
+ * by the same butterfly, and the block sums are added in block order starting
+ * from 0.  (The reference adds the terms into delta[v] one by one in the
+ * order of its distance sort; sums in different orders differ in the last
+ * bits.) */
 typedef struct { double d; uint32_t v; } or_dv;
 static int cmp_dv(const void *a, const void *b) {
     const or_dv *x = (const or_dv *)a, *y = (const or_dv *)b;
@@ -499,30 +511,44 @@ static int cmp_dv(const void *a, const void *b) {
     if (x->d > y->d) return 1;
     return (x->v > y->v) - (x->v < y->v);
 }
+static double or_butterfly32(double *v) {
+    for (int h = 16; h > 0; h >>= 1)
+        for (int i = 0; i < h; i++) v[i] = v[i] + v[i + h];
+    return v[0];
+}
+typedef struct { double w; uint32_t c; } or_wc;
+static int cmp_wc(const void *a, const void *b) {
+    const or_wc *x = (const or_wc *)a, *y = (const or_wc *)b;
+    if (x->w < y->w) return -1;
+    if (x->w > y->w) return 1;
+    return (x->c > y->c) - (x->c < y->c);
+}
 
 #define OR_BC_BODY(DT, WT, DIJKSTRA, TIGHT, INF_TEST)                                     \
-    uint64_t *rrow = (uint64_t *)calloc((size_t)n + 1, 8);                                \
-    uint32_t *rsrc = (uint32_t *)malloc(sizeof(uint32_t) * (row[n] ? row[n] : 1));        \
-    WT *rw = (WT *)malloc(sizeof(WT) * (row[n] ? row[n] : 1));                            \
+    const uint64_t m = row[n];                                                            \
+    uint32_t *scol = (uint32_t *)malloc(sizeof(uint32_t) * (m ? m : 1));                  \
+    WT *sw = (WT *)malloc(sizeof(WT) * (m ? m : 1));                                      \
+    or_wc *tmp = (or_wc *)malloc(sizeof(or_wc) * (m ? m : 1));                            \
     DT *dist = (DT *)malloc(sizeof(DT) * n);                                              \
     uint64_t *sig = (uint64_t *)malloc(8 * (size_t)n);                                    \
     double *del = (double *)malloc(8 * (size_t)n);                                        \
     or_dv *ord = (or_dv *)malloc(sizeof(or_dv) * n);                                      \
-    uint64_t *cur = (uint64_t *)malloc(8 * ((size_t)n + 1));                              \
     int rc = 0;                                                                           \
-    if (!rrow || !rsrc || !rw || !dist || !sig || !del || !ord || !cur) rc = -1;          \
+    if (!scol || !sw || !tmp || !dist || !sig || !del || !ord) rc = -1;                   \
     for (uint32_t v = 0; v < n && !rc; v++) bc[v] = 0.0;                                  \
-    /* in-edges (transpose) */                                                            \
-    for (uint32_t u = 0; u < n && !rc; u++)                                               \
-        for (uint64_t e = row[u]; e < row[u + 1]; e++) rrow[col[e] + 1]++;                \
-    for (uint32_t v = 0; v < n && !rc; v++) rrow[v + 1] += rrow[v];                       \
-    for (uint32_t v = 0; v <= n && !rc; v++) cur[v] = rrow[v];                            \
-    for (uint32_t u = 0; u < n && !rc; u++)                                               \
-        for (uint64_t e = row[u]; e < row[u + 1]; e++) {                                  \
-            uint64_t p = cur[col[e]]++;                                                   \
-            rsrc[p] = u;                                                                  \
-            rw[p] = w[e];                                                                 \
+    /* rows sorted by (weight, column) at their own positions */                          \
+    for (uint32_t u = 0; u < n && !rc; u++) {                                             \
+        const uint64_t b = row[u], d = row[u + 1] - row[u];                               \
+        for (uint64_t i = 0; i < d; i++) {                                                \
+            tmp[b + i].w = (double)w[b + i];                                              \
+            tmp[b + i].c = col[b + i];                                                    \
         }                                                                                 \
+        qsort(tmp + b, d, sizeof(or_wc), cmp_wc);                                         \
+        for (uint64_t i = 0; i < d; i++) {                                                \
+            scol[b + i] = tmp[b + i].c;                                                   \
+            sw[b + i] = (WT)tmp[b + i].w;                                                 \
+        }                                                                                 \
+    }                                                                                     \
     for (uint32_t k = 0; k < nsrc && !rc; k++) {                                          \
         const uint32_t s = srcs ? srcs[k] : k;                                            \
         if (DIJKSTRA(n, row, col, w, s, dist)) { rc = -1; break; }                        \
@@ -536,28 +562,44 @@ static int cmp_dv(const void *a, const void *b) {
         sig[s] = 1;                                                                       \
         for (uint32_t i = 0; i < n; i++) {                                                \
             const uint32_t x = ord[i].v;                                                  \
-            if (x == s || INF_TEST(dist[x])) continue;                                    \
-            for (uint64_t e = rrow[x]; e < rrow[x + 1]; e++) {                            \
-                const uint32_t v = rsrc[e];                                               \
-                if (!INF_TEST(dist[v]) && TIGHT(dist[v], rw[e], dist[x])) sig[x] += sig[v]; \
-            }                                                                             \
+            if (INF_TEST(dist[x])) continue;                                              \
+            for (uint64_t e = row[x]; e < row[x + 1]; e++)                                \
+                if (TIGHT(dist[x], sw[e], dist[scol[e]])) sig[scol[e]] += sig[x];         \
         }                                                                                 \
         for (uint32_t i = n; i-- > 0;) {                                                  \
             const uint32_t x = ord[i].v;                                                  \
-            if (x == s || INF_TEST(dist[x])) continue;                                    \
-            for (uint64_t e = rrow[x]; e < rrow[x + 1]; e++) {                            \
-                const uint32_t v = rsrc[e];                                               \
-                if (v != s && !INF_TEST(dist[v]) && TIGHT(dist[v], rw[e], dist[x]))       \
-                    del[v] += (1.0 + del[x]) * (double)(int64_t)sig[v] / (double)(int64_t)sig[x]; \
+            if (x == s || INF_TEST(dist[x]) || row[x] == row[x + 1]) continue;            \
+            const double sx = (double)(int64_t)sig[x];                                    \
+            const uint64_t wb = row[x] / 32, nw = (row[x + 1] - 1) / 32 + 1 - wb;         \
+            double acc = 0.0;                                                             \
+            for (uint64_t b = 0; b * 32 < nw; b++) {                                      \
+                double q[32];                                                             \
+                for (int j = 0; j < 32; j++) {                                            \
+                    q[j] = 0.0;                                                           \
+                    if (b * 32 + j >= nw) continue;                                       \
+                    const uint64_t W = wb + b * 32 + j;                                   \
+                    double t[32];                                                         \
+                    for (int i = 0; i < 32; i++) {                                        \
+                        const uint64_t e = W * 32 + i;                                    \
+                        t[i] = 0.0;                                                       \
+                        if (e < row[x] || e >= row[x + 1]) continue;                      \
+                        const uint32_t y = scol[e];                                       \
+                        if (TIGHT(dist[x], sw[e], dist[y]))                               \
+                            t[i] = (1.0 + del[y]) * sx / (double)(int64_t)sig[y];         \
+                    }                                                                     \
+                    q[j] = or_butterfly32(t);                                             \
+                }                                                                         \
+                acc += or_butterfly32(q);                                                 \
             }                                                                             \
+            del[x] = acc;                                                                 \
         }                                                                                 \
         for (uint32_t v = 0; v < n; v++)                                                  \
             if (v != s) bc[v] += del[v];                                                  \
     }                                                                                     \
-    free(rrow); free(rsrc); free(rw); free(dist); free(sig); free(del); free(ord); free(cur); \
+    free(scol); free(sw); free(tmp); free(dist); free(sig); free(del); free(ord);         \
     return rc;
 
-#define OR_TIGHT_U32(du, w, dv) ((uint64_t)(du) + (w) == (uint64_t)(dv))
+#define OR_TIGHT_U32(du, w, dv) ((dv) != OR_UNREACHED_U32 && (uint64_t)(du) + (w) == (uint64_t)(dv))
 #define OR_INF_U32(d) ((d) == OR_UNREACHED_U32)
 static int or_tight_f32(float du, float w, float dv) { volatile float s = du + w; return s == dv; }
 static int or_tight_f64(double du, double w, double dv) { volatile double s = du + w; return s == dv; }
