@@ -72,6 +72,7 @@ PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "heavy", 3: "relax", 4: "pe
                8: "bc_count", 9: "bc_forward", 10: "bc_backward", 11: "bc_backward_words"}
 F_TRACE = 0x2
 F_NO_SOLO = 0x4
+F_BC_SINGLE = 0x20
 F_FEATURES = 0x8
 F_LEARNED = 0x10
 N_FEAT = 16

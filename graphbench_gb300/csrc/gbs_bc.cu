@@ -302,13 +302,6 @@ __device__ __forceinline__ void append_order(const BcArgs &a, bool take, uint32_
     }
 }
 
-// One tight edge of the COUNT pass.
-__device__ __forceinline__ void count_tight(const BcArgs &a, uint32_t e, uint32_t v, unsigned long long &tight_n) {
-    atomicAdd(a.indeg + v, 1u);
-    atomicOr(a.mask + (e >> 5), 1u << (e & 31u));
-    ++tight_n;
-}
-
 // COUNT over mask words: the warp takes kCountUnroll words per round, one
 // position per lane, all loads of the round in flight before any is used.
 // The row owning position W * 32 + l is ne_rows[k0 + popc(starts & bits 1..l)].
@@ -789,6 +782,19 @@ __global__ void __launch_bounds__(kTPB, 1) bc_dag(BcArgs a) {
     }
 }
 
+// Batched shortest paths hand back plain distances (uint32 / float32 bits,
+// UINT32_MAX / +inf unreached); the DAG passes read state words.
+template <bool F32>
+__global__ void k_pack_dist(const uint32_t *__restrict__ dist, uint32_t n, unsigned long long *__restrict__ dp) {
+    const uint32_t unreached = F32 ? 0x7F800000u : 0xFFFFFFFFu;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t d = dist[v];
+        dp[v] = d == unreached ? kUnreached : (unsigned long long)d << 32;
+    }
+}
+
+constexpr uint32_t kBcBatch = 64;   // sources per batched shortest-path launch
+
 struct BcState {
     unsigned long long *sigma = nullptr;
     double *delta = nullptr;
@@ -982,17 +988,8 @@ gbs_status run_bc(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_p
     const void *kfn = bc_kernel(g->wtype);
     gbs_bc_stats tot{};
     double dag_ms = 0.0;
-    for (uint32_t i = 0; i < k; ++i) {
-        const uint32_t src = sources ? sources[i] : i;
-        gbs_stats one{};
-        st = run_sssp(g, src, &p, nullptr, nullptr, &one);
-        if (st != GBS_OK) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return st;
-        }
-        tot.sssp_ms += one.device_ms;
-        tot.edges_reached += one.edges_reached;
+    // one DAG launch on the distances now in the workspace's state words
+    auto dag = [&](uint32_t src) -> gbs_status {
         a.source = src;
         void *args[] = {&a};
         GBS_CUDA(cudaEventRecord(e0, s));
@@ -1000,11 +997,71 @@ gbs_status run_bc(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_p
         GBS_CUDA(cudaMemsetAsync(b->mask, 0, sizeof(uint32_t) * b->mask_words, s));
         GBS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(b->blocks), dim3(kTPB), args, 0, s));
         GBS_CUDA(cudaEventRecord(e1, s));
-        // the next source's SSSP synchronises the stream; time this one now
         GBS_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
         GBS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         dag_ms += ms;
+        return GBS_OK;
+    };
+    const bool batched = g->wtype != GBS_WEIGHT_F64 && k > 1 &&
+                         !(p.flags & (GBS_F_BC_SINGLE | GBS_F_LEARNED));
+    if (!batched) {
+        for (uint32_t i = 0; i < k && st == GBS_OK; ++i) {
+            const uint32_t src = sources ? sources[i] : i;
+            gbs_stats one{};
+            st = run_sssp(g, src, &p, nullptr, nullptr, &one);
+            if (st != GBS_OK) break;
+            tot.sssp_ms += one.device_ms;
+            tot.edges_reached += one.edges_reached;
+            st = dag(src);
+        }
+    } else {
+        // up to kBcBatch sources per batched launch, distances kept on the
+        // device; each source's DAG passes then run on its distances
+        gbs_batch_params bp{};
+        bp.delta = p.delta;
+        bp.light = p.light;
+        bp.flags = p.flags & GBS_F_NO_SOLO;
+        bp.wait_limit_ms = p.wait_limit_ms;
+        bp.solo_entries = p.solo_entries;
+        bp.solo_descs = p.solo_descs;
+        bp.inline_edges = p.inline_edges;
+        const uint32_t chunk = std::min(k, kBcBatch);
+        uint32_t *bdist = nullptr;
+        if (cudaMalloc(&bdist, sizeof(uint32_t) * (size_t)chunk * g->n) != cudaSuccess) {
+            cudaGetLastError();
+            st = fail(GBS_ERR_NO_MEMORY, "betweenness: no room for the batched distances");
+        }
+        std::vector<uint32_t> cs(chunk);
+        for (uint32_t i0 = 0; i0 < k && st == GBS_OK; i0 += chunk) {
+            const uint32_t cnt = std::min(chunk, k - i0);
+            for (uint32_t j = 0; j < cnt; ++j) cs[j] = sources ? sources[i0 + j] : i0 + j;
+            gbs_plan *plan = nullptr;
+            st = gbs_plan_sources(g, cs.data(), cnt, &bp, bdist, nullptr, &plan);
+            if (st != GBS_OK) break;
+            gbs_batch_stats bs{};
+            st = gbs_plan_launch(plan);
+            if (st == GBS_OK) st = gbs_plan_wait(plan, &bs, nullptr);
+            gbs_plan_destroy(plan);
+            if (st != GBS_OK) break;
+            tot.sssp_ms += bs.device_ms;
+            tot.edges_reached += bs.edges_reached;
+            const int tb = 256, eb = std::max(1, std::min<int>((g->n + tb - 1) / tb, g->sms * 8));
+            for (uint32_t j = 0; j < cnt && st == GBS_OK; ++j) {
+                if (g->wtype == GBS_WEIGHT_F32)
+                    k_pack_dist<true><<<eb, tb, 0, s>>>(bdist + (size_t)j * g->n, g->n, g->ws.dp);
+                else
+                    k_pack_dist<false><<<eb, tb, 0, s>>>(bdist + (size_t)j * g->n, g->n, g->ws.dp);
+                if (cudaGetLastError() != cudaSuccess) st = fail(GBS_ERR_CUDA, "betweenness: launch failed");
+                else st = dag(cs[j]);
+            }
+        }
+        cudaFree(bdist);
+    }
+    if (st != GBS_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return st;
     }
     BcTotals t{};
     BcCtl last{};

@@ -87,6 +87,8 @@ typedef struct gbs_params {
 #define GBS_F_FEATURES 0x8u  /* record the controller inputs at every bucket start (gbs_features) */
 #define GBS_F_LEARNED 0x10u  /* bucket widths from the graph's learned controller
                                 (gbs_graph_set_controller) */
+#define GBS_F_BC_SINGLE 0x20u /* gbs_bc: one single-source launch per source instead of
+                                batched launches of up to 64 sources */
 /* Failure-path test: one CTA never arrives at the first grid barrier, so every
  * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
  * wait_limit_ms and the device stays usable.  Never set in normal use. */
@@ -181,7 +183,10 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
  * when a vertex has several shortest-path predecessors).  Weights must be
  * positive (GBS_ERR_INVALID_ARG otherwise).  bc_out: n doubles in host
  * memory.  params: the schedule of the shortest-path runs (NULL: the
- * default); the result does not depend on it.
+ * default); the result does not depend on it.  uint32 / float32 graphs solve
+ * the shortest paths of up to 64 sources in one batched launch (as
+ * gbs_plan_sources) unless GBS_F_BC_SINGLE or GBS_F_LEARNED is set; float64
+ * graphs run one source at a time.
  */
 typedef struct gbs_bc_stats {
     double device_ms;        /* CUDA-event time of all shortest-path runs and DAG passes */

@@ -288,6 +288,24 @@ def test_gpu_bc_device_output_and_schedules(gb, orc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("wtype", ["u32", "f32"])
+def test_gpu_bc_batched_equals_single(wtype, gb, orc):
+    """Shortest paths solved in batched launches (more sources than one batch
+    holds) or one source at a time give the same distances, hence the same
+    betweenness, bit for bit."""
+    _need_gpu(gb)
+    from oracle import gen
+    row, col, w = gen.rmat(10, 16, 41, wtype, 1, 12)
+    src = gen.sample_sources(row, 70, 3)
+    with gb.Graph(row, col, w) as g:
+        bb, sb = g.betweenness(src)
+        bs, ss = g.betweenness(src, flags=gb.F_BC_SINGLE)
+    assert np.array_equal(bb, bs)
+    assert np.array_equal(bb, orc.betweenness(row, col, w, src))
+    assert sb["edges_reached"] == ss["edges_reached"] and sb["tight_edges"] == ss["tight_edges"]
+
+
+@pytest.mark.gpu
 def test_gpu_bc_rmat16_sampled(gb, orc):
     """A larger graph (R-MAT scale 16, 1M edges) with sampled sources."""
     _need_gpu(gb)
