@@ -24,6 +24,9 @@ Beside the plain kernel, on the same resident graph and the same sources:
              (gbs_plan_sources with the parameters gbs_autotune_plan_sources
              picked), dist/pred of every source kept on the device
 Each reports GTEPS and its ratio to the plain value.
+  betweenness  gbs_bc over 16 of the sources (batched shortest paths, then
+             the path-count / dependency passes per source), with a bit-exact
+             check of one more source against the oracle at full scale
 
 Multi-GPU: one process per GPU (torchrun); every rank runs the whole workload
 on its own GPU (replicas: a single SSSP does not shard); value = sum over
@@ -256,6 +259,37 @@ def arm_batched(gb, g, srcs, reps: int = 5):
             "path": "gbs_plan_sources + gbs_plan_launch (CUDA graph), outputs on the device"}
 
 
+def arm_betweenness(gb, g, hg, srcs, cpu: bool, n_src: int = 16):
+    """Betweenness centrality (gbs_bc) over the first n_src sources of the
+    workload: batched shortest paths + the DAG passes, rate in edges out of
+    reached vertices per second summed over sources.  One more source is run
+    alone and compared bit for bit with the oracle's Brandes restatement, whose
+    single-thread time on it is the CPU baseline."""
+    src = [int(x) for x in srcs[:n_src]]
+    g.betweenness(src[:2])
+    bc, st = g.betweenness(src)
+    k = len(src)
+    out = {"value": st["edges_reached"] / st["device_ms"] / 1e6, "unit": "GTEPS",
+           "sources": k, "ms_per_source": st["device_ms"] / k,
+           "sssp_ms_per_source": st["sssp_ms"] / k, "dag_ms_per_source": st["dag_ms"] / k,
+           "max_levels": st["max_levels"], "tight_edges_per_source": st["tight_edges"] / k,
+           "path": "gbs_bc (C ABI): batched gbs_plan_sources launches of up to 64 sources, then one "
+                   "cooperative bc_dag launch per source; result accumulated on the device"}
+    if cpu:
+        import oracle
+        one = [int(srcs[n_src % len(srcs)])]
+        ours, st1 = g.betweenness(one)
+        t0 = time.perf_counter()
+        ref = oracle.betweenness(hg.row, hg.col, hg.w, one)
+        secs = time.perf_counter() - t0
+        out["parity_one_source"] = {"bit_identical": bool(np.array_equal(ours, ref)),
+                                    "max_rel": float(np.max(np.abs(ours - ref) / np.maximum(1.0, np.abs(ref))))}
+        out["cpu_baseline"] = {"value": st1["edges_reached"] / secs / 1e9, "unit": "GTEPS", "cores": 1,
+                               "kind": "port", "sample": f"1 source, oracle Brandes (Dijkstra + path counts + "
+                                                         f"dependencies), {secs:.1f} s"}
+    return out
+
+
 # ----------------------------------------------------------------- our arm
 def run_ours(args):
     world, rank, local = dist_env()
@@ -378,6 +412,12 @@ def run_ours(args):
                     arm = {"value": None, "error": str(e)}
                 result[name] = arm
                 log(f"[rank 0] {name}: {arm.get('value')}")
+        if world == 1 and not args.no_bc:
+            try:
+                result["betweenness"] = arm_betweenness(gb, g, hg, srcs, cpu=not args.no_cpu_baseline)
+            except Exception as e:  # pragma: no cover
+                result["betweenness"] = {"value": None, "error": str(e)}
+            log(f"[rank 0] betweenness: {result['betweenness'].get('value')}")
         if world == 1 and not args.no_cpu_baseline:
             try:
                 result["cpu_baseline"] = cpu_baseline_port(hg, srcs, st0["delta_used"], args.cpu_budget_s)
@@ -489,6 +529,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-arms", action="store_true", help="skip the learned / autotuned / batched arms")
+    ap.add_argument("--no-bc", action="store_true", help="skip the betweenness measurement")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-scale", type=int, default=16)
     ap.add_argument("--ref-procs", type=int, default=16)

@@ -302,6 +302,31 @@ __device__ __forceinline__ void append_order(const BcArgs &a, bool take, uint32_
     }
 }
 
+// L2 policies for COUNT: the edge stream is read once (evict first), the
+// state words it gathers are reused across the whole pass (evict last).
+__device__ __forceinline__ unsigned long long l2_policy_first() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long l2_policy_last() {
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint2 ld_edge_once(const uint2 *ptr, unsigned long long pol) {
+    uint2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(v.x), "=r"(v.y) : "l"(ptr), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_state_keep(const unsigned long long *ptr,
+                                                            unsigned long long pol) {
+    unsigned long long v;
+    asm volatile("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(ptr), "l"(pol));
+    return v;
+}
+
 // COUNT over mask words: the warp takes kCountUnroll words per round, one
 // position per lane, all loads of the round in flight before any is used.
 // The row owning position W * 32 + l is ne_rows[k0 + popc(starts & bits 1..l)].
@@ -311,6 +336,7 @@ __device__ __forceinline__ void count_words(const BcArgs &a, uint32_t W0, uint32
                                             unsigned long long &tight_n) {
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t below = (2u << lane) - 1u;
+    const unsigned long long pol_first = l2_policy_first(), pol_last = l2_policy_last();
     for (uint32_t Wb = W0; Wb < a.n_words; Wb += stride * kCountUnroll) {
         uint32_t e[kCountUnroll], u[kCountUnroll];
         uint2 ew[kCountUnroll];
@@ -327,14 +353,14 @@ __device__ __forceinline__ void count_words(const BcArgs &a, uint32_t W0, uint32
                 const uint2 o = __ldg(a.wown + W);
                 u[j] = o.x + (uint32_t)__popc(o.y & below);
             }
-            ew[j] = ok[j] ? __ldg(a.adj + e[j]) : make_uint2(0u, 0u);
+            ew[j] = ok[j] ? ld_edge_once(a.adj + e[j], pol_first) : make_uint2(0u, 0u);
         }
 #pragma unroll
         for (uint32_t j = 0; j < kCountUnroll; ++j) u[j] = ok[j] ? __ldg(a.ne_rows + u[j]) : 0u;
 #pragma unroll
         for (uint32_t j = 0; j < kCountUnroll; ++j) {
-            pu[j] = ok[j] ? __ldg(a.dp + u[j]) : kUnreached;
-            pv[j] = ok[j] ? __ldg(a.dp + ew[j].x) : kUnreached;
+            pu[j] = ok[j] ? ld_state_keep(a.dp + u[j], pol_last) : kUnreached;
+            pv[j] = ok[j] ? ld_state_keep(a.dp + ew[j].x, pol_last) : kUnreached;
         }
 #pragma unroll
         for (uint32_t j = 0; j < kCountUnroll; ++j)
