@@ -35,7 +35,9 @@ F_NO_STATS = 0x1
 EXPORTS = [
     "gbs_status_string", "gbs_last_error", "gbs_abi_version", "gbs_device_available",
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
-    "gbs_sssp_multi", "gbs_bc", "gbs_bc_device", "gbs_trace", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
+    "gbs_sssp_multi", "gbs_bc", "gbs_bc_device", "gbs_trace",
+    "gbs_read_text", "gbs_parse_text", "gbs_read_bin", "gbs_parse_bin", "gbs_device_csr_info",
+    "gbs_device_csr_export", "gbs_graph_from_device_csr", "gbs_device_csr_destroy", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
     "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
     "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
     "gbs_autotune", "gbs_autotune_plan_sources", "gbs_autotune_plan_pack",
@@ -102,6 +104,16 @@ class BcStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class IngestInfo(ctypes.Structure):
+    _fields_ = [("v_num", ctypes.c_int64), ("e_num", ctypes.c_int64), ("offset", ctypes.c_int64),
+                ("g_v_size", ctypes.c_int64), ("records", ctypes.c_uint64), ("edges", ctypes.c_uint64),
+                ("duplicates", ctypes.c_uint64), ("read_ms", ctypes.c_double), ("parse_ms", ctypes.c_double),
+                ("build_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class CsrView(ctypes.Structure):
@@ -174,6 +186,17 @@ def _load() -> ctypes.CDLL:
                                  ctypes.POINTER(Stats)]
     L.gbs_bc.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
     L.gbs_bc_device.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
+    L.gbs_read_text.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(IngestInfo)]
+    L.gbs_parse_text.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(P),
+                                 ctypes.POINTER(IngestInfo)]
+    L.gbs_read_bin.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(P),
+                               ctypes.POINTER(IngestInfo)]
+    L.gbs_parse_bin.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+                                ctypes.POINTER(P), ctypes.POINTER(IngestInfo)]
+    L.gbs_device_csr_info.argtypes = [P, P, P]
+    L.gbs_device_csr_export.argtypes = [P, P, P, P]
+    L.gbs_graph_from_device_csr.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
+    L.gbs_device_csr_destroy.argtypes = [P]
     L.gbs_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
     L.gbs_host_free.argtypes = [P]
     L.gbs_device_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
@@ -373,6 +396,18 @@ class Graph:
     def from_host(cls, g: HostGraph) -> "Graph":
         return cls(g.row, g.col, g.w)
 
+    @classmethod
+    def _adopt(cls, handle: ctypes.c_void_p, wtype: int) -> "Graph":
+        g = cls.__new__(cls)
+        n, m = ctypes.c_uint32(), ctypes.c_uint64()
+        wt, mw = ctypes.c_int(), ctypes.c_double()
+        _check(lib.gbs_graph_info(handle, ctypes.byref(n), ctypes.byref(m), ctypes.byref(wt), ctypes.byref(mw),
+                                  None), "gbs_graph_info")
+        g.n, g.m, g.wtype = n.value, m.value, wtype
+        g.dist_dtype = {W_F32: np.float32, W_U32: np.uint32, W_F64: np.float64}[wtype]
+        g._h = handle
+        return g
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib.gbs_graph_destroy(self._h)
@@ -522,6 +557,82 @@ class Graph:
                                   _ptr(pred) if pred is not None else None, ctypes.byref(st)),
                "gbs_sssp_multi")
         return dist, pred, st.as_dict()
+
+
+# ------------------------------------------------------------ graph ingest
+DIR_RECV, DIR_SEND = 0, 1
+
+
+class DeviceCsr:
+    """A graph read on the GPU (gbs_read_text / gbs_read_bin and the parse_*
+    variants over bytes), laid out as the reference's readers lay out their
+    t_csr (graph/csr.c): rows in file order, weights where the reference
+    stores them."""
+
+    def __init__(self, handle: ctypes.c_void_p, info: IngestInfo):
+        self._h = handle
+        self.info = info.as_dict()
+        n, m = ctypes.c_uint32(), ctypes.c_uint64()
+        _check(lib.gbs_device_csr_info(handle, ctypes.byref(n), ctypes.byref(m)), "gbs_device_csr_info")
+        self.n, self.m = n.value, m.value
+
+    @classmethod
+    def read_text(cls, path, direction: int = DIR_SEND) -> "DeviceCsr":
+        h, info = ctypes.c_void_p(), IngestInfo()
+        _check(lib.gbs_read_text(str(path).encode(), direction, ctypes.byref(h), ctypes.byref(info)), "gbs_read_text")
+        return cls(h, info)
+
+    @classmethod
+    def parse_text(cls, data: bytes, direction: int = DIR_SEND) -> "DeviceCsr":
+        h, info = ctypes.c_void_p(), IngestInfo()
+        _check(lib.gbs_parse_text(data, len(data), direction, ctypes.byref(h), ctypes.byref(info)), "gbs_parse_text")
+        return cls(h, info)
+
+    @classmethod
+    def read_bin(cls, path, direction: int = DIR_SEND, target_offset: int = 1, dedup: bool = False) -> "DeviceCsr":
+        h, info = ctypes.c_void_p(), IngestInfo()
+        _check(lib.gbs_read_bin(str(path).encode(), direction, target_offset, int(bool(dedup)), ctypes.byref(h),
+                                ctypes.byref(info)), "gbs_read_bin")
+        return cls(h, info)
+
+    @classmethod
+    def parse_bin(cls, data: bytes, direction: int = DIR_SEND, target_offset: int = 1,
+                  dedup: bool = False) -> "DeviceCsr":
+        h, info = ctypes.c_void_p(), IngestInfo()
+        _check(lib.gbs_parse_bin(data, len(data), direction, target_offset, int(bool(dedup)), ctypes.byref(h),
+                                 ctypes.byref(info)), "gbs_parse_bin")
+        return cls(h, info)
+
+    def export(self):
+        """(row_offsets uint64[n+1] exclusive, cols uint32[m], weights float64[m])."""
+        row = np.empty(self.n + 1, dtype=np.uint64)
+        col = np.empty(self.m, dtype=np.uint32)
+        w = np.empty(self.m, dtype=np.float64)
+        _check(lib.gbs_device_csr_export(self._h, _ptr(row), _ptr(col), _ptr(w)), "gbs_device_csr_export")
+        return row, col, w
+
+    def graph(self, wtype: int = W_F64) -> "Graph":
+        """A resident graph built on the device (rows sorted by (weight, column))."""
+        h = ctypes.c_void_p()
+        _check(lib.gbs_graph_from_device_csr(self._h, wtype, ctypes.byref(h)), "gbs_graph_from_device_csr")
+        return Graph._adopt(h, wtype)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.gbs_device_csr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 # ------------------------------------------------ reference-shaped mirror

@@ -686,6 +686,34 @@ gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_
     return GBS_OK;
 }
 
+gbs_status graph_shell(uint32_t n, uint64_t m, gbs_weight_type wtype, double max_w, double mean_w,
+                       bool zero_w, gbs_graph **out) {
+    int dev = 0;
+    GBS_CUDA(cudaGetDevice(&dev));
+    gbs_graph *g = new gbs_graph();
+    g->n = n;
+    g->m = m;
+    g->wtype = wtype;
+    g->max_w = max_w;
+    g->mean_w = mean_w;
+    g->zero_w = zero_w;
+    g->device = dev;
+    cudaError_t e;
+    if ((e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        free_graph(g);
+        return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (auto &ev : g->ev) {
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+            free_graph(g);
+            return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    *out = g;
+    return GBS_OK;
+}
+
 }  // namespace gbs
 
 // ===================================================================== C ABI
@@ -737,31 +765,15 @@ gbs_status gbs_graph_create(uint32_t n, uint64_t m, const uint64_t *row_offsets,
         wsum += wtype == GBS_WEIGHT_U32   ? (double)((const uint32_t *)weights)[e]
                 : wtype == GBS_WEIGHT_F32 ? (double)((const float *)weights)[e]
                                           : ((const double *)weights)[e];
-    int dev = 0;
-    GBS_CUDA(cudaGetDevice(&dev));
-    gbs_graph *g = new gbs_graph();
-    g->n = n;
-    g->m = m;
-    g->wtype = wtype;
-    g->max_w = max_w;
-    g->mean_w = m ? wsum / (double)m : 0.0;
+    bool zero_w = false;
     // rows are sorted by weight: a zero weight is the first of its row
-    for (uint32_t v = 0; v < n && !g->zero_w; ++v)
+    for (uint32_t v = 0; v < n && !zero_w; ++v)
         if (row32[v] < row32[v + 1])
-            g->zero_w = wtype == GBS_WEIGHT_F64 ? w64[row32[v]] == 0ull : adj[row32[v]].y == 0u;
-    g->device = dev;
+            zero_w = wtype == GBS_WEIGHT_F64 ? w64[row32[v]] == 0ull : adj[row32[v]].y == 0u;
+    gbs_graph *g = nullptr;
+    st = graph_shell(n, m, wtype, max_w, m ? wsum / (double)m : 0.0, zero_w, &g);
+    if (st != GBS_OK) return st;
     cudaError_t e;
-    if ((e = cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess) {
-        free_graph(g);
-        return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
-    }
-    for (auto &ev : g->ev) {
-        if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
-            free_graph(g);
-            return fail(GBS_ERR_CUDA, cudaGetErrorString(e));
-        }
-    }
     if ((e = cudaMalloc(&g->d_row, sizeof(uint32_t) * (n + 1))) != cudaSuccess ||
         (e = cudaMalloc(&g->d_adj, sizeof(uint2) * (m ? m : 1))) != cudaSuccess ||
         (e = cudaMemcpy(g->d_row, row32.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice)) !=

@@ -113,6 +113,12 @@ void free_workspace(Workspace &w);
 // Resident CTAs of the persistent kernels on one SM (0 if they cannot run).
 int persistent_ctas_per_sm(gbs_weight_type wt, bool batch);
 
+// A graph handle without device arrays (stream, events, device attributes);
+// the caller fills d_row / d_adj / d_w64 (free_graph releases them).
+gbs_status graph_shell(uint32_t n, uint64_t m, gbs_weight_type wtype, double max_w, double mean_w, bool zero_w,
+                       gbs_graph **out);
+void free_graph(gbs_graph *g);
+
 // Allocates the single-source workspace of a graph on first use.
 gbs_status ensure_workspace(gbs_graph *g);
 // One single-source run (learned controller and its guard included) with the

@@ -170,6 +170,62 @@ gbs_status gbs_sssp_multi(gbs_graph *g, const uint32_t *sources, uint32_t k,
                           gbs_stats *stats);
 
 /*
+ * Graph ingest on the GPU: the reference's readers (graph/csr.c) with the
+ * parsing and the CSR build done on the device.  A gbs_device_csr holds the
+ * graph exactly as the reference's t_csr would: n = v_num rows, each row's
+ * edges in file order, and the weights where the reference puts them.
+ *
+ * gbs_read_text / gbs_parse_text: scan_csr_idx + read_graph_csr
+ *   (graph/csr.c:4-202).  Lines "p <name> v_num e_num offset g_v_size" and
+ *   "a v_id v_to weight"; other lines are skipped; the first e_num "a" lines
+ *   are read.  GBS_DIR_SEND: row = v_id - offset, column = v_to - 1;
+ *   GBS_DIR_RECV: row = v_to - offset, column = v_id - 1.  Weights: the k-th
+ *   "a" line's v_to / v_num, stored at CSR position k (the reference's
+ *   edge_info[e_num_read]; the same as the edge's own weight only for files
+ *   sorted by row); the line's third number is ignored, as there.
+ * gbs_read_bin / gbs_parse_bin: read_csr_bin (graph/csr.c:211-299).  int64
+ *   v_num, e_num, offset, g_v_size, then e_num int64 (from, to) pairs.
+ *   SEND: row = from - offset, column = to - target_offset; RECV: row = to -
+ *   offset, column = from - target_offset (target_offset: the reference's
+ *   OFFSET, 1 in its default build, 0 in its Graph500 build).  Weight of CSR
+ *   position p: 0.1 (p even) or 0.2 (p odd).  dedup != 0 first drops every
+ *   (from, to) pair that appeared earlier in the file (remove_duplicate,
+ *   partition/csr_partition_bin_mpi.c:47-105).
+ * Rows and columns outside [0, v_num) are rejected (GBS_ERR_INVALID_ARG,
+ * gbs_last_error names the edge).
+ */
+#define GBS_DIR_RECV 0
+#define GBS_DIR_SEND 1
+typedef struct gbs_device_csr gbs_device_csr;
+typedef struct gbs_ingest_info {
+    int64_t v_num, e_num, offset, g_v_size;   /* the file's header */
+    uint64_t records;        /* "a" lines (text) or pairs (binary) in the file */
+    uint64_t edges;          /* edges in the CSR */
+    uint64_t duplicates;     /* pairs dropped by dedup */
+    double read_ms;          /* host file read (gbs_read_*) */
+    double parse_ms;         /* device: copy in, parse / split, duplicate removal */
+    double build_ms;         /* device: CSR build */
+} gbs_ingest_info;
+
+gbs_status gbs_read_text(const char *path, int direction, gbs_device_csr **out, gbs_ingest_info *info);
+gbs_status gbs_parse_text(const char *bytes, size_t len, int direction, gbs_device_csr **out,
+                          gbs_ingest_info *info);
+gbs_status gbs_read_bin(const char *path, int direction, int64_t target_offset, int dedup,
+                        gbs_device_csr **out, gbs_ingest_info *info);
+gbs_status gbs_parse_bin(const void *bytes, size_t len, int direction, int64_t target_offset, int dedup,
+                         gbs_device_csr **out, gbs_ingest_info *info);
+gbs_status gbs_device_csr_info(const gbs_device_csr *c, uint32_t *n, uint64_t *m);
+/* Host copies: row_offsets n+1 exclusive offsets, cols m, weights m (any may be NULL). */
+gbs_status gbs_device_csr_export(const gbs_device_csr *c, uint64_t *row_offsets, uint32_t *cols,
+                                 double *weights);
+/* A resident graph built on the device from the CSR (rows sorted by (weight,
+ * column) as gbs_graph_create sorts them).  GBS_WEIGHT_F64 keeps the weights
+ * exactly; F32 rounds them; U32 needs integer weights.  The CSR may be
+ * destroyed afterwards. */
+gbs_status gbs_graph_from_device_csr(const gbs_device_csr *c, gbs_weight_type wtype, gbs_graph **out);
+gbs_status gbs_device_csr_destroy(gbs_device_csr *c);
+
+/*
  * Betweenness centrality (Brandes over shortest paths), the computation of
  * run_bc (btwcentral/csr_bc.c:16-64) on a resident graph instead of a file:
  * for every source s (sources[0..k), or every vertex when sources is NULL)

@@ -198,6 +198,9 @@ def ref_lib(variant: str = "serial") -> ctypes.CDLL:
         L.gbref_sssp_list.restype = ctypes.c_int
         L.gbref_bc.argtypes = [_i64, _i64, _P, _P, _P, _i64, _P, _dbl, ctypes.c_int, _P, _P, _P]
         L.gbref_bc.restype = ctypes.c_int
+        L.gbref_read_graph.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _i64,
+                                       _i64, _P, _P, _P, _P]
+        L.gbref_read_graph.restype = ctypes.c_int
         _ref_libs[variant] = L
     return _ref_libs[variant]
 
@@ -280,6 +283,24 @@ def ref_bc(row, col, w, sources=None, delta: float = 0.1, dedup: bool = False):
     return bc, int(dups[0]), float(secs[0])
 
 
+def ref_read_graph(path, binary: bool, direction: int, cap_n: int = 1 << 20, cap_m: int = 1 << 22):
+    """The reference's own readers on a file (graph/csr.c: scan_csr_idx +
+    read_graph_csr for text, read_csr_bin for binary; direction 1 = SEND,
+    0 = RECV).  Returns (row_end int64[n] inclusive, col int64[m],
+    weight float64[m]) exactly as the reference leaves them in its t_csr."""
+    p = Path(path).resolve()
+    nm = np.zeros(2, dtype=np.int64)
+    re = np.zeros(cap_n + 1, dtype=np.int64)
+    cl = np.zeros(cap_m + 1, dtype=np.int64)
+    wt = np.zeros(cap_m + 1, dtype=np.float64)
+    rc = ref_lib("serial").gbref_read_graph(str(p.parent).encode() + b"/", p.name.encode(), int(bool(binary)),
+                                            int(direction), cap_n, cap_m, _ptr(nm), _ptr(re), _ptr(cl), _ptr(wt))
+    if rc != 0:
+        raise RuntimeError(f"reference reader failed (code {rc})")
+    n, m = int(nm[0]), int(nm[1])
+    return re[:n].copy(), cl[:m].copy(), wt[:m].copy()
+
+
 def betweenness(row, col, w, sources=None) -> np.ndarray:
     """Brandes betweenness over shortest paths summed over `sources` (all
     vertices when None), restating btwcentral/csr_bc.c:16-123 with each tight
@@ -295,3 +316,95 @@ def betweenness(row, col, w, sources=None) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"oracle betweenness failed ({rc})")
     return bc
+
+
+# ------------------------------------------------------------ graph readers
+def _text_records(data: bytes):
+    """Header and "a" records of a text graph, line by line (graph/csr.c:
+    scan_csr_idx :136-202 and read_graph_csr :4-60 read the same tokens)."""
+    hdr = None
+    recs = []
+    for raw in data.split(b"\n"):
+        tok = raw.split()
+        if not tok:
+            continue
+        if tok[0] == b"p" and hdr is None:
+            if recs:
+                raise ValueError("an \"a\" line before the \"p\" line")
+            hdr = [int(t) for t in tok[2:6]]
+        elif tok[0] == b"a":
+            if hdr is None:
+                raise ValueError("an \"a\" line before the \"p\" line")
+            if len(tok) < 4:
+                raise ValueError("an \"a\" line without three integers")
+            recs.append((int(tok[1]), int(tok[2]), int(tok[3])))
+    if hdr is None:
+        raise ValueError("no \"p\" line")
+    return hdr, recs[: hdr[1]]
+
+
+def _stable_csr(rows, cols, n):
+    """Rows filled in input order (the reference's v_idx_tmp placement)."""
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    order = np.argsort(rows, kind="stable")
+    row = np.zeros(n + 1, dtype=np.uint64)
+    np.add.at(row, rows + 1, 1)
+    return np.cumsum(row).astype(np.uint64), cols[order].astype(np.uint32)
+
+
+def read_text(data: bytes, direction: int):
+    """Restates scan_csr_idx + read_graph_csr (graph/csr.c:4-202) on the bytes
+    of a text graph.  direction 1 = SEND (row = v_id - offset, column = v_to - 1),
+    0 = RECV (row = v_to - offset, column = v_id - 1).  Weights: the k-th
+    record's v_to / v_num at CSR position k (edge_info[e_num_read], :46).
+    Returns (row_offsets uint64[n+1] exclusive, cols uint32[m], weights
+    float64[m], header)."""
+    hdr, recs = _text_records(data)
+    v_num, offset = hdr[0], hdr[2]
+    a = np.array([r[0] for r in recs], dtype=np.int64)
+    b = np.array([r[1] for r in recs], dtype=np.int64)
+    if direction == 1:
+        rows, cols = a - offset, b - 1
+    else:
+        rows, cols = b - offset, a - 1
+    if len(recs) and (rows.min() < 0 or rows.max() >= v_num or cols.min() < 0 or cols.max() >= v_num):
+        raise ValueError("a row or column outside [0, v_num)")
+    row, col = _stable_csr(rows, cols, v_num)
+    w = b.astype(np.float64) / float(v_num)
+    return row, col, w, hdr
+
+
+def dedup_pairs(a, b):
+    """remove_duplicate (partition/csr_partition_bin_mpi.c:47-105): keep the
+    first occurrence of every (from, to) pair, in file order."""
+    seen = set()
+    keep = []
+    for i, p in enumerate(zip(a.tolist(), b.tolist())):
+        if p not in seen:
+            seen.add(p)
+            keep.append(i)
+    keep = np.array(keep, dtype=np.int64)
+    return a[keep], b[keep]
+
+
+def read_bin(data: bytes, direction: int, target_offset: int = 1, dedup: bool = False):
+    """Restates read_csr_bin (graph/csr.c:211-299): int64 header v_num, e_num,
+    offset, g_v_size and e_num int64 (from, to) pairs.  SEND: row = from -
+    offset, column = to - target_offset; RECV: row = to - offset, column = from
+    - target_offset.  Weight of CSR position p: 0.1 if p is even, else 0.2."""
+    hdr = np.frombuffer(data[:32], dtype="<i8").tolist()
+    v_num, e_num, offset = hdr[0], hdr[1], hdr[2]
+    pairs = np.frombuffer(data[32:32 + 16 * e_num], dtype="<i8").reshape(-1, 2)
+    a, b = pairs[:, 0].copy(), pairs[:, 1].copy()
+    if dedup:
+        a, b = dedup_pairs(a, b)
+    if direction == 1:
+        rows, cols = a - offset, b - target_offset
+    else:
+        rows, cols = b - offset, a - target_offset
+    if len(a) and (rows.min() < 0 or rows.max() >= v_num or cols.min() < 0 or cols.max() >= v_num):
+        raise ValueError("a row or column outside [0, v_num)")
+    row, col = _stable_csr(rows, cols, v_num)
+    w = np.where(np.arange(len(col)) % 2 == 0, 0.1, 0.2)
+    return row, col, w, hdr

@@ -322,3 +322,66 @@ int gbref_bc(int64_t n, int64_t m, const int64_t *row, const int64_t *col, const
     munmap(map, map_bytes);
     return rc;
 }
+
+/* graph/csr.c readers on the file dir/file: scan_csr_idx + read_graph_csr
+ * (text, :4-202) when bin == 0, read_csr_bin (:211-299) when bin == 1, with
+ * type SEND (1) or RECV (0).  Copies out v_size, e_size, the inclusive row
+ * ends vet_idx, edge_idx and edge_info[].edge_weight (at most cap_n / cap_m
+ * entries).  Runs in a forked child: the readers allocate and never free, and
+ * stop the process on a missing file. */
+void scan_csr_idx(t_csr *graph, char *file, char *dir, sint type);
+void read_graph_csr(t_csr *graph, char *file, char *dir, sint type);
+void read_csr_bin(t_csr *graph, char *file, char *dir, sint type, int myrank);
+
+int gbref_read_graph(const char *dir, const char *file, int bin, int type, int64_t cap_n, int64_t cap_m,
+                     int64_t *nm_out, int64_t *row_end, int64_t *col, double *w) {
+    size_t map_bytes = sizeof(ref_result) + 16 + 8 * (size_t)(cap_n + 2 * cap_m + 3);
+    void *map = mmap(NULL, map_bytes, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
+    if (map == MAP_FAILED) return -10;
+    ref_result *res = (ref_result *)map;
+    int64_t *nm = (int64_t *)((char *)map + sizeof(ref_result));
+    int64_t *re = nm + 2;
+    int64_t *cl = re + cap_n + 1;
+    double *wt = (double *)(cl + cap_m + 1);
+    res->status = -1;
+    fflush(NULL);
+    pid_t pid = fork();
+    if (pid < 0) { munmap(map, map_bytes); return -11; }
+    if (pid == 0) {
+        quiet_stdout();
+        t_csr *gs = (t_csr *)calloc(1, sizeof(t_csr));
+        char d[4096], f[4096];
+        snprintf(d, sizeof d, "%s", dir);
+        snprintf(f, sizeof f, "%s", file);
+        if (bin) {
+            read_csr_bin(gs, f, d, (sint)type, 0);
+        } else {
+            scan_csr_idx(gs, f, d, (sint)type);
+            read_graph_csr(gs, f, d, (sint)type);
+        }
+        nm[0] = gs->v_size;
+        nm[1] = gs->e_size;
+        if (gs->v_size > cap_n || gs->e_size > cap_m) { res->status = 2; _exit(0); }
+        for (int64_t v = 0; v < gs->v_size; v++) re[v] = gs->vet_idx[v];
+        for (int64_t e = 0; e < gs->e_size; e++) {
+            cl[e] = gs->edge_idx[e];
+            wt[e] = gs->edge_info[e].edge_weight;
+        }
+        res->status = 0;
+        _exit(0);
+    }
+    int st = 0;
+    waitpid(pid, &st, 0);
+    int rc = 0;
+    nm_out[0] = nm[0];
+    nm_out[1] = nm[1];
+    if (!WIFEXITED(st) || WEXITSTATUS(st) != 0 || res->status != 0) {
+        rc = WIFSIGNALED(st) ? -100 - WTERMSIG(st) : (res->status == 2 ? -13 : -12);
+    } else {
+        memcpy(row_end, re, 8 * (size_t)nm[0]);
+        memcpy(col, cl, 8 * (size_t)nm[1]);
+        memcpy(w, wt, 8 * (size_t)nm[1]);
+    }
+    munmap(map, map_bytes);
+    return rc;
+}

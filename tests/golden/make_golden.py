@@ -271,6 +271,89 @@ def check_bc(have_ref: bool):
     return out
 
 
+# ------------------------------------------------------------ graph files
+INGEST_DIR = HERE / "ingest"
+
+# The reference reads whitespace-separated tokens, so a comment holding a
+# lone "a" or "p" token is taken for a record (its reader crashed on one);
+# the comments below avoid such tokens.
+HAND_TEXT = (b"c hand-made graph: comments, blank lines, CRLF endings, records out of\r\n"
+             b"c row order, leading blanks, and one record past e_num\r\n"
+             b"p sp 6 7 1 6\r\n"
+             b"\r\n"
+             b"a 3 1 7\r\n"
+             b"a 1 2 4\r\n"
+             b"  a 1 6 9\r\n"
+             b"a 2 3 1\r\n"
+             b"c in the middle\r\n"
+             b"a 6 4 2\r\n"
+             b"a\t3 4 8\r\n"
+             b"a 5 5 3\r\n"
+             b"a 4 1 5\r\n")
+
+
+def _bin_bytes(v_num, offset, pairs):
+    import struct
+    out = struct.pack("<4q", v_num, len(pairs), offset, v_num)
+    for a, b in pairs:
+        out += struct.pack("<2q", a, b)
+    return out
+
+
+def ingest_files():
+    """(name, kind, bytes): hand-made and seeded graph files."""
+    files = [("hand.txt", "text", HAND_TEXT)]
+    u, v = gen.rmat_edges(8, 8, 17)          # raw samples: self loops and repeats included
+    u = u.astype(np.int64)
+    v = v.astype(np.int64)
+    rng = np.random.default_rng(5)
+    w = rng.integers(1, 100, len(u))
+    lines = [b"c R-MAT scale 8 samples, file order as generated", b"p sp 256 %d 1 256" % len(u)]
+    lines += [b"a %d %d %d" % (a + 1, b + 1, c) for a, b, c in zip(u.tolist(), v.tolist(), w.tolist())]
+    files.append(("rmat8.txt", "text", b"\n".join(lines) + b"\n"))
+    files.append(("hand.bin", "bin", _bin_bytes(5, 1, [(3, 1), (1, 2), (1, 5), (2, 3), (5, 4), (3, 4), (1, 2),
+                                                        (3, 1), (4, 5)])))
+    files.append(("rmat8.bin", "bin", _bin_bytes(256, 1, list(zip((u + 1).tolist(), (v + 1).tolist())))))
+    return files
+
+
+def make_ingest(have_ref: bool):
+    """Expected CSRs of the graph files: the reference's own readers
+    (scan_csr_idx + read_graph_csr, read_csr_bin) when it is built, checked
+    against the oracle's restatement; duplicate removal restated (the
+    reference's remove_duplicate needs its MPI driver) and then read by the
+    reference's read_csr_bin."""
+    INGEST_DIR.mkdir(exist_ok=True)
+    out = []
+    for name, kind, data in ingest_files():
+        (INGEST_DIR / name).write_bytes(data)
+        for direction in (1, 0):
+            for dedup in ((False, True) if kind == "bin" else (False,)):
+                if kind == "text":
+                    row, col, w, hdr = oracle.read_text(data, direction)
+                else:
+                    row, col, w, hdr = oracle.read_bin(data, direction, 1, dedup)
+                rec = dict(file=name, kind=kind, direction=direction, dedup=dedup, n=int(len(row) - 1),
+                           m=int(len(col)), row_sha=sha(row), col_sha=sha(col), w_sha=sha(w))
+                if have_ref:
+                    path = INGEST_DIR / name
+                    if dedup:
+                        a = np.frombuffer(data[32:], dtype="<i8").reshape(-1, 2)
+                        x, y = oracle.dedup_pairs(a[:, 0].copy(), a[:, 1].copy())
+                        tmp = Path("/tmp") / f"gb_dedup_{name}"
+                        tmp.write_bytes(_bin_bytes(hdr[0], hdr[2], list(zip(x.tolist(), y.tolist()))))
+                        path = tmp
+                    re, cl, wt = oracle.ref_read_graph(path, kind == "bin", direction)
+                    assert np.array_equal(row[1:].astype(np.int64), re), (name, direction, "rows")
+                    assert np.array_equal(col.astype(np.int64), cl), (name, direction, "cols")
+                    assert np.array_equal(w, wt), (name, direction, "weights")
+                    rec["reference"] = "bit-exact"
+                if len(col) <= 16:
+                    rec.update(row=row.tolist(), col=col.tolist(), w=w.tolist())
+                out.append(rec)
+    return out
+
+
 def main():
     have_ref = build_ref.stage()
     if have_ref:
@@ -278,6 +361,8 @@ def main():
     known = check_known(have_ref)
     seeded = check_seeded(have_ref)
     bc = check_bc(have_ref)
+    ingest = make_ingest(have_ref)
+    (HERE / "ingest_golden.json").write_text(json.dumps(ingest, indent=1) + "\n")
     (HERE / "bc_golden.json").write_text(json.dumps(bc) + "\n")
     (HERE / "known_answer.json").write_text(json.dumps(known, indent=1) + "\n")
     (HERE / "seeded.json").write_text(json.dumps(seeded, indent=1) + "\n")
