@@ -359,3 +359,190 @@ void gbs_compat_allow_float32(int allow) { g_allow_f32 = allow != 0; }
 void gbs_compat_set_exit(int exit_on_error) { g_exit_on_error = exit_on_error != 0; }
 
 gbs_status gbs_compat_status(void) { return g_status; }
+
+/* ------------------------------------------------------------ readers
+ * graph/csr.c's readers with the parsing and CSR build on the GPU
+ * (gbs_read_text / gbs_read_bin); the t_csr is filled exactly as the
+ * reference fills it.  scan_csr_idx reads the whole file and keeps the edge
+ * arrays for the read_graph_csr call that follows on the same t_csr.       */
+
+/* The reference's OFFSET for binary targets (include/graph.h:28-32). */
+#ifndef GBS_COMPAT_BIN_OFFSET
+#define GBS_COMPAT_BIN_OFFSET 1
+#endif
+
+typedef struct {
+    const t_csr *gs;
+    uint32_t *col;
+    double *w;
+    uint64_t m;
+} pending_t;
+static pending_t g_pending;
+
+static void *alloc64(size_t bytes) {
+    void *p = NULL;
+    if (posix_memalign(&p, 64, bytes ? bytes : 64) != 0) return NULL;
+    return p;
+}
+
+static void join_path(char *out, size_t cap, const char *dir, const char *file) {
+    snprintf(out, cap, "%s%s", dir ? dir : "", file ? file : "");
+}
+
+static int export_csr(gbs_device_csr *c, uint64_t **row, uint32_t **col, double **w, uint32_t *n, uint64_t *m) {
+    gbs_status st = gbs_device_csr_info(c, n, m);
+    if (st != GBS_OK) return st;
+    *row = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)*n + 1));
+    *col = (uint32_t *)malloc(sizeof(uint32_t) * (*m ? *m : 1));
+    *w = (double *)malloc(sizeof(double) * (*m ? *m : 1));
+    if (!*row || !*col || !*w) return GBS_ERR_NO_MEMORY;
+    return gbs_device_csr_export(c, *row, *col, *w);
+}
+
+static void fill_rows(t_csr *graph, const uint64_t *row, uint32_t n, int bin) {
+    graph->vet_idx = (lint *)alloc64(sizeof(lint) * (n ? n : 1));
+    graph->vet_info = (t_vi *)alloc64(sizeof(t_vi) * (n ? n : 1));
+    for (uint32_t v = 0; v < n; ++v) {
+        const lint deg = (lint)(row[v + 1] - row[v]);
+        graph->vet_idx[v] = (lint)row[v + 1];            /* inclusive end */
+        /* scan_csr_idx (:163-168, :195-196) / read_csr_bin (:238-243) */
+        graph->vet_info[v].weight = bin ? INFINITY : 1.0;
+        graph->vet_info[v].wb = 0;
+        graph->vet_info[v].recip = bin ? 0.0 : 1.0 / (double)deg;
+        graph->vet_info[v].vet_deg = bin ? 0 : deg;
+    }
+}
+
+static void fill_edges(t_csr *graph, const uint32_t *col, const double *w, uint64_t m) {
+    const size_t cap = (size_t)(graph->e_size > (lint)m ? graph->e_size : (lint)m);
+    graph->edge_idx = (lint *)alloc64(sizeof(lint) * (cap ? cap : 1));
+    graph->edge_info = (t_e *)alloc64(sizeof(t_e) * (cap ? cap : 1));
+    memset(graph->edge_idx, 0, sizeof(lint) * (cap ? cap : 1));
+    memset(graph->edge_info, 0, sizeof(t_e) * (cap ? cap : 1));
+    for (uint64_t e = 0; e < m; ++e) {
+        graph->edge_idx[e] = (lint)col[e];
+        graph->edge_info[e].edge_weight = w[e];
+    }
+}
+
+void scan_csr_idx(t_csr *graph, char *file, char *dir, sint type) {
+    char path[4096];
+    join_path(path, sizeof path, dir, file);
+    gbs_device_csr *c = NULL;
+    gbs_ingest_info info;
+    uint64_t *row = NULL;
+    uint32_t *col = NULL, n = 0;
+    double *w = NULL;
+    uint64_t m = 0;
+    gbs_status st = gbs_read_text(path, type ? GBS_DIR_SEND : GBS_DIR_RECV, &c, &info);
+    if (st == GBS_OK) st = export_csr(c, &row, &col, &w, &n, &m);
+    if (c) gbs_device_csr_destroy(c);
+    if (st == GBS_OK) {
+        graph->offset = info.offset;
+        graph->v_size = info.v_num;
+        graph->e_size = info.e_num;
+        graph->global_v_size = info.g_v_size;
+        fill_rows(graph, row, n, 0);
+        pthread_mutex_lock(&g_mu);
+        free(g_pending.col);
+        free(g_pending.w);
+        g_pending.gs = graph;
+        g_pending.col = col;
+        g_pending.w = w;
+        g_pending.m = m;
+        col = NULL;
+        w = NULL;
+        pthread_mutex_unlock(&g_mu);
+    }
+    free(row);
+    free(col);
+    free(w);
+    set_status(st, "scan_csr_idx", st == GBS_OK ? NULL : gbs_last_error());
+}
+
+void read_graph_csr(t_csr *graph, char *file, char *dir, sint type) {
+    pthread_mutex_lock(&g_mu);
+    int have = g_pending.gs == graph && g_pending.col;
+    pending_t p = g_pending;
+    if (have) memset(&g_pending, 0, sizeof g_pending);
+    pthread_mutex_unlock(&g_mu);
+    gbs_status st = GBS_OK;
+    if (!have) {   /* not preceded by scan_csr_idx on this t_csr: read again */
+        char path[4096];
+        join_path(path, sizeof path, dir, file);
+        gbs_device_csr *c = NULL;
+        gbs_ingest_info info;
+        uint64_t *row = NULL;
+        uint32_t n = 0;
+        st = gbs_read_text(path, type ? GBS_DIR_SEND : GBS_DIR_RECV, &c, &info);
+        if (st == GBS_OK) st = export_csr(c, &row, &p.col, &p.w, &n, &p.m);
+        if (c) gbs_device_csr_destroy(c);
+        free(row);
+    }
+    if (st == GBS_OK) fill_edges(graph, p.col, p.w, p.m);
+    free(p.col);
+    free(p.w);
+    set_status(st, "read_graph_csr", st == GBS_OK ? NULL : gbs_last_error());
+}
+
+void read_csr_bin(t_csr *graph, char *file, char *dir, sint type, int myrank) {
+    (void)myrank;
+    char path[4096];
+    join_path(path, sizeof path, dir, file);
+    gbs_device_csr *c = NULL;
+    gbs_ingest_info info;
+    uint64_t *row = NULL;
+    uint32_t *col = NULL, n = 0;
+    double *w = NULL;
+    uint64_t m = 0;
+    gbs_status st = gbs_read_bin(path, type ? GBS_DIR_SEND : GBS_DIR_RECV, GBS_COMPAT_BIN_OFFSET, 0, &c, &info);
+    if (st == GBS_OK) st = export_csr(c, &row, &col, &w, &n, &m);
+    if (c) gbs_device_csr_destroy(c);
+    if (st == GBS_OK) {
+        graph->offset = info.offset;
+        graph->v_size = info.v_num;
+        graph->e_size = info.e_num;
+        graph->global_v_size = info.g_v_size;
+        fill_rows(graph, row, n, 1);
+        fill_edges(graph, col, w, m);
+    }
+    free(row);
+    free(col);
+    free(w);
+    set_status(st, "read_csr_bin", st == GBS_OK ? NULL : gbs_last_error());
+}
+
+/* ------------------------------------------------------------ run_bc
+ * btwcentral/csr_bc.c:16-64: read the graph (read_csr_bin when the
+ * program's `bin` flag is set, else the text reader, type SEND), Brandes over
+ * every vertex as source on the GPU (gbs_bc), and the reference's printout.
+ * The graph goes to the device straight from the device CSR. */
+extern int bin __attribute__((weak));
+
+void run_bc(char *file, char *dir) {
+    char path[4096];
+    join_path(path, sizeof path, dir, file);
+    gbs_device_csr *c = NULL;
+    gbs_ingest_info info;
+    gbs_graph *g = NULL;
+    double *bc = NULL;
+    uint32_t n = 0;
+    gbs_status st = (&bin && bin) ? gbs_read_bin(path, GBS_DIR_SEND, GBS_COMPAT_BIN_OFFSET, 0, &c, &info)
+                                  : gbs_read_text(path, GBS_DIR_SEND, &c, &info);
+    if (st == GBS_OK) st = gbs_device_csr_info(c, &n, NULL);
+    if (st == GBS_OK) st = gbs_graph_from_device_csr(c, GBS_WEIGHT_F64, &g);
+    if (c) gbs_device_csr_destroy(c);
+    if (st == GBS_OK) {
+        bc = (double *)malloc(sizeof(double) * (n ? n : 1));
+        if (!bc) st = GBS_ERR_NO_MEMORY;
+    }
+    if (st == GBS_OK) st = gbs_bc(g, NULL, n, NULL, bc, NULL);
+    if (st == GBS_OK) {
+        printf("the final result for betweeness centrality is:\n");
+        for (uint32_t i = 0; i < n; i++) printf("%lld:%lf ", (long long)i + 1, bc[i]);
+        printf("\n");
+    }
+    if (g) gbs_graph_destroy(g);
+    free(bc);
+    set_status(st, "run_bc", st == GBS_OK ? NULL : gbs_last_error());
+}

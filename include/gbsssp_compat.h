@@ -2,12 +2,12 @@
  * gbsssp_compat.h -- link-compatible replacements for GRAPHBENCH's SSSP entry
  * points, implemented in libgbsssp_compat.so on top of libgbsssp (gbsssp.h).
  *
- * A program built against the reference keeps its own CSR readers
- * (scan_csr_idx / read_graph_csr / read_csr_bin, graph/csr.c) and its
- * predecessor lists, drops the reference's SSSP objects
- * (sssp/csr_sspath_array.c, sssp/csr_sspath.c) and links this library
- * instead: the two functions below have the reference's names, signatures and
- * argument meaning, and read and write the same structures.
+ * A program built against the reference drops the reference's SSSP objects
+ * (sssp/csr_sspath_array.c, sssp/csr_sspath.c) -- and, if it wants them on
+ * the GPU, its CSR readers (graph/csr.c) and betweenness
+ * (btwcentral/csr_bc.c) -- and links this library instead: the functions
+ * below have the reference's names, signatures and argument meaning, and read
+ * and write the same structures.
  *
  *   run_sspath_arr  sssp/csr_sspath_array.c:149-151 (called from
  *                   main/main.c:223; declared in no header there)
@@ -91,6 +91,35 @@ typedef struct list_elem *p_list;
 
 void run_sspath_arr(t_csr *gs, p_list *predecesor, lint source, double delta);
 void run_sspath(t_csr *gs, p_list *predecesor, lint source, double delta);
+
+/*
+ * The readers of graph/csr.c with parsing and CSR build on the GPU
+ * (gbs_read_text / gbs_read_bin); the t_csr is filled as the reference fills
+ * it: v_size, e_size, offset and global_v_size from the header, vet_idx the
+ * inclusive row ends, rows in file order, edge_info[].edge_weight where the
+ * reference stores it, vet_info as scan_csr_idx (weight 1, recip 1/degree,
+ * vet_deg the degree) or read_csr_bin (weight INFINITY, recip 0, vet_deg 0)
+ * leaves it.  Arrays are 64-byte aligned (posix_memalign); the reference never
+ * frees them either.  A program that keeps graph/csr.c linked keeps its own
+ * readers (its definitions take precedence).
+ *
+ *   scan_csr_idx    graph/csr.c:133-202 (reads the whole file; the edges are
+ *                   kept for the read_graph_csr call that follows)
+ *   read_graph_csr  graph/csr.c:4-60
+ *   read_csr_bin    graph/csr.c:211-299 (targets shifted by
+ *                   GBS_COMPAT_BIN_OFFSET, the reference's OFFSET, 1 unless
+ *                   the library is built with -DGBS_COMPAT_BIN_OFFSET=0)
+ *   run_bc          btwcentral/csr_bc.c:16-64: reads the graph (read_csr_bin
+ *                   when the program's global `bin` is set, else the text
+ *                   reader, SEND), betweenness over every vertex on the GPU
+ *                   (gbs_bc, float64 weights), and the reference's printout
+ *                   ("the final result for betweeness centrality is:" then
+ *                   "i:value " for i = 1..n).  Each tight edge counts once.
+ */
+void scan_csr_idx(t_csr *graph, char *file, char *dir, sint type);
+void read_graph_csr(t_csr *graph, char *file, char *dir, sint type);
+void read_csr_bin(t_csr *graph, char *file, char *dir, sint type, int myrank);
+void run_bc(char *file, char *dir);
 
 /* Library-specific controls (no counterpart in the reference). */
 void gbs_compat_forget(const t_csr *gs);        /* drop the cached device copy of gs */

@@ -199,3 +199,77 @@ def test_run_sspath_arr_float32_grid(driver, tmp_path, gb, orc):
     assert r.returncode == 0 and "status 0" in r.stdout, r.stderr
     dist, _ = read_output(out, a.n)
     assert np.array_equal(dist, orc.dijkstra(a.row, a.col, a.w, 0).astype(np.float64))
+
+
+# ------------------------------------------------- readers and run_bc
+GOLD = ROOT / "tests" / "golden"
+
+
+@pytest.fixture(scope="module")
+def io_driver(tmp_path_factory):
+    out = tmp_path_factory.mktemp("compat_io") / "compat_io_driver"
+    subprocess.run(["gcc", "-O2", "-std=c11", "-I", str(INCLUDE), str(ROOT / "tests" / "compat_io_driver.c"),
+                    "-o", str(out), "-L", str(PKG), "-lgbsssp_compat", "-lgbsssp",
+                    f"-Wl,-rpath,{PKG}"], check=True, capture_output=True, text=True)
+    return out
+
+
+def test_compat_io_driver_links(io_driver):
+    assert io_driver.exists()
+
+
+def _read_tcsr(path):
+    raw = np.fromfile(path, dtype=np.uint8)
+    hdr = raw[:32].view(np.int64)
+    n, m = int(hdr[0]), int(hdr[1])
+    per_v = raw[32:32 + 40 * n].reshape(n, 40)
+    vet_idx = per_v[:, 0:8].copy().view(np.int64).ravel()
+    weight = per_v[:, 8:16].copy().view(np.float64).ravel()
+    wb = per_v[:, 16:24].copy().view(np.float64).ravel()
+    recip = per_v[:, 24:32].copy().view(np.float64).ravel()
+    deg = per_v[:, 32:40].copy().view(np.int64).ravel()
+    per_e = raw[32 + 40 * n:].reshape(m, 16)
+    col = per_e[:, 0:8].copy().view(np.int64).ravel()
+    ew = per_e[:, 8:16].copy().view(np.float64).ravel()
+    return hdr.tolist(), vet_idx, weight, wb, recip, deg, col, ew
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,kind", [("hand.txt", "text"), ("rmat8.txt", "text"), ("hand.bin", "bin"),
+                                       ("rmat8.bin", "bin")])
+@pytest.mark.parametrize("direction", [1, 0])
+def test_compat_readers_fill_tcsr_like_the_reference(name, kind, direction, io_driver, tmp_path, orc):
+    out = tmp_path / "tcsr.bin"
+    r = subprocess.run([str(io_driver), kind, str(GOLD / "ingest") + "/", name, str(direction), str(out)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    hdr, vet_idx, weight, wb, recip, deg, col, ew = _read_tcsr(out)
+    data = (GOLD / "ingest" / name).read_bytes()
+    row, c2, w2, h2 = orc.read_text(data, direction) if kind == "text" else orc.read_bin(data, direction)
+    assert hdr == [h2[0], h2[1], h2[2], h2[3]]
+    assert np.array_equal(vet_idx, row[1:].astype(np.int64))
+    assert np.array_equal(col[: len(c2)], c2.astype(np.int64)) and np.array_equal(ew[: len(w2)], w2)
+    d = np.diff(row.astype(np.int64))
+    if kind == "text":   # scan_csr_idx's vertex fields
+        assert np.all(weight == 1.0) and np.all(wb == 0) and np.array_equal(deg, d)
+        with np.errstate(divide="ignore"):
+            assert np.array_equal(recip, 1.0 / d.astype(np.float64))
+    else:                # read_csr_bin's
+        assert np.all(np.isinf(weight)) and np.all(wb == 0) and np.all(recip == 0) and np.all(deg == 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["hand.txt", "rmat8.txt"])
+def test_compat_run_bc_prints_the_reference_report(name, io_driver, orc):
+    """run_bc(file, dir): the reference's printout, values equal to the
+    oracle's Brandes on the graph the reference's text reader builds."""
+    r = subprocess.run([str(io_driver), "bc", str(GOLD / "ingest") + "/", name], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == "the final result for betweeness centrality is:"
+    pairs = [t.split(":") for t in lines[1].split()]
+    row, col, w, _ = orc.read_text((GOLD / "ingest" / name).read_bytes(), 1)
+    ours = orc.betweenness(row, col, w)
+    assert [int(p[0]) for p in pairs] == list(range(1, len(row)))
+    assert [p[1] for p in pairs] == ["%f" % x for x in ours]
