@@ -37,7 +37,8 @@ EXPORTS = [
     "gbs_graph_create", "gbs_graph_destroy", "gbs_graph_info", "gbs_sssp", "gbs_sssp_device",
     "gbs_sssp_multi", "gbs_bc", "gbs_bc_device", "gbs_trace",
     "gbs_read_text", "gbs_parse_text", "gbs_read_bin", "gbs_parse_bin", "gbs_device_csr_info",
-    "gbs_device_csr_export", "gbs_graph_from_device_csr", "gbs_device_csr_destroy", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
+    "gbs_device_csr_export", "gbs_graph_from_device_csr", "gbs_device_csr_destroy",
+    "gbs_pagerank", "gbs_device_csr_transpose", "gbs_sssp_noalloc", "gbs_host_alloc", "gbs_host_free",
     "gbs_pack_create", "gbs_pack_destroy", "gbs_pack_info", "gbs_plan_sources", "gbs_plan_pack",
     "gbs_plan_launch", "gbs_plan_wait", "gbs_plan_destroy",
     "gbs_autotune", "gbs_autotune_plan_sources", "gbs_autotune_plan_pack",
@@ -111,6 +112,19 @@ class IngestInfo(ctypes.Structure):
                 ("g_v_size", ctypes.c_int64), ("records", ctypes.c_uint64), ("edges", ctypes.c_uint64),
                 ("duplicates", ctypes.c_uint64), ("read_ms", ctypes.c_double), ("parse_ms", ctypes.c_double),
                 ("build_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PagerankParams(ctypes.Structure):
+    _fields_ = [("random_jump", ctypes.c_double), ("threshold", ctypes.c_double),
+                ("max_iters", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class PagerankStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("converged", ctypes.c_uint32),
+                ("device_ms", ctypes.c_double), ("edges", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -197,6 +211,8 @@ def _load() -> ctypes.CDLL:
     L.gbs_device_csr_export.argtypes = [P, P, P, P]
     L.gbs_graph_from_device_csr.argtypes = [P, ctypes.c_int, ctypes.POINTER(P)]
     L.gbs_device_csr_destroy.argtypes = [P]
+    L.gbs_pagerank.argtypes = [P, ctypes.POINTER(PagerankParams), P, ctypes.POINTER(PagerankStats)]
+    L.gbs_device_csr_transpose.argtypes = [P, ctypes.POINTER(P)]
     L.gbs_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
     L.gbs_host_free.argtypes = [P]
     L.gbs_device_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(P)]
@@ -610,6 +626,34 @@ class DeviceCsr:
         w = np.empty(self.m, dtype=np.float64)
         _check(lib.gbs_device_csr_export(self._h, _ptr(row), _ptr(col), _ptr(w)), "gbs_device_csr_export")
         return row, col, w
+
+    def transpose(self) -> "DeviceCsr":
+        h = ctypes.c_void_p()
+        _check(lib.gbs_device_csr_transpose(self._h, ctypes.byref(h)), "gbs_device_csr_transpose")
+        return DeviceCsr(h, IngestInfo())
+
+    def pagerank(self, random_jump: float = 0.0, threshold: float = 0.0, max_iters: int = 0):
+        """PageRank with this CSR as the in-edge lists (gbs_pagerank).
+        Returns (rank float64[n], stats dict)."""
+        p = PagerankParams(random_jump, threshold, max_iters, 0)
+        st = PagerankStats()
+        out = np.empty(self.n, dtype=np.float64)
+        _check(lib.gbs_pagerank(self._h, ctypes.byref(p), _ptr(out), ctypes.byref(st)), "gbs_pagerank")
+        return out, st.as_dict()
+
+    @classmethod
+    def from_arrays(cls, row, col, w=None) -> "DeviceCsr":
+        """A device CSR from host arrays (exclusive offsets, columns, weights),
+        through the binary reader's in-memory form."""
+        row = np.asarray(row, dtype=np.int64)
+        col = np.asarray(col, dtype=np.int64)
+        n = len(row) - 1
+        src = np.repeat(np.arange(n, dtype=np.int64), np.diff(row))
+        pairs = np.empty((len(col), 2), dtype="<i8")
+        pairs[:, 0] = src + 1
+        pairs[:, 1] = col + 1
+        data = np.array([n, len(col), 1, n], dtype="<i8").tobytes() + pairs.tobytes()
+        return cls.parse_bin(data, DIR_SEND, 1, False)
 
     def graph(self, wtype: int = W_F64) -> "Graph":
         """A resident graph built on the device (rows sorted by (weight, column))."""

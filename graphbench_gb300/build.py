@@ -24,7 +24,7 @@ COMPAT_LIB = PKG / "libgbsssp_compat.so"
 COMPAT_SOURCES = ["host/compat.c"]
 
 CUDA_SOURCES = ["csrc/gbs_api.cu", "csrc/gbs_batch.cu", "csrc/gbs_tune.cu", "csrc/gbs_mlp.cu", "csrc/gbs_noalloc.cu",
-                "csrc/gbs_bc.cu", "csrc/gbs_ingest.cu"]
+                "csrc/gbs_bc.cu", "csrc/gbs_ingest.cu", "csrc/gbs_pagerank.cu"]
 C_SOURCES = ["host/gen.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

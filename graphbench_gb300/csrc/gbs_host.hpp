@@ -66,6 +66,16 @@ struct gbs_graph {
     void *bc = nullptr;
 };
 
+// A CSR on the device as the reference's readers lay it out (gbs_ingest.cu):
+// rows in file order, weights where the reference stores them.
+struct gbs_device_csr {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    unsigned long long *d_row = nullptr;   // exclusive offsets, n + 1
+    uint32_t *d_col = nullptr;
+    double *d_w = nullptr;
+};
+
 namespace gbs {
 
 // Bucket width and light bound of one run, as the kernel uses them.

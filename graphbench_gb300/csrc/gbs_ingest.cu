@@ -40,14 +40,6 @@
 
 #include "gbs_host.hpp"
 
-struct gbs_device_csr {
-    uint32_t n = 0;
-    uint64_t m = 0;
-    unsigned long long *d_row = nullptr;   // exclusive offsets, n + 1
-    uint32_t *d_col = nullptr;
-    double *d_w = nullptr;
-};
-
 namespace gbs {
 namespace {
 

@@ -226,6 +226,38 @@ gbs_status gbs_graph_from_device_csr(const gbs_device_csr *c, gbs_weight_type wt
 gbs_status gbs_device_csr_destroy(gbs_device_csr *c);
 
 /*
+ * PageRank, the reference's iteration (pagerank/pagerank_mpi.c:667-1043 on
+ * one node) as a pull over an IN-edge CSR (row v lists the u with an edge
+ * u -> v: gbs_read_text(path, GBS_DIR_RECV, ...) as the reference reads it,
+ * or gbs_device_csr_transpose of an out-edge CSR).  weight = 1, recip =
+ * 1 / out-degree (the count of each vertex among the columns), wb =
+ * random_jump, diff = weight * recip; each iteration wb[v] += (1 -
+ * random_jump) * sum of diff[u] over the in-edges, diff[v] = (wb[v] -
+ * weight[v]) * recip[v], weight = wb, until no |diff| exceeds threshold.
+ * rank_out: n doubles (host), the final weight.  params may be NULL:
+ * random_jump 0.3 and threshold 1e-6 (RDM_JMP, THRESH, include/graph.h:17-18).
+ */
+typedef struct gbs_pagerank_params {
+    double random_jump;      /* <= 0: 0.3 */
+    double threshold;        /* <= 0: 1e-6 */
+    uint32_t max_iters;      /* 0: 10000 */
+    uint32_t reserved;
+} gbs_pagerank_params;
+
+typedef struct gbs_pagerank_stats {
+    uint32_t iterations;
+    uint32_t converged;      /* 1: stopped on the threshold, 0: on max_iters */
+    double device_ms;        /* CUDA events around the iterations */
+    uint64_t edges;
+} gbs_pagerank_stats;
+
+gbs_status gbs_pagerank(const gbs_device_csr *in_edges, const gbs_pagerank_params *params, double *rank_out,
+                        gbs_pagerank_stats *stats);
+/* The transposed CSR (row v lists the rows that list v, in row order),
+ * weights carried along. */
+gbs_status gbs_device_csr_transpose(const gbs_device_csr *c, gbs_device_csr **out);
+
+/*
  * Betweenness centrality (Brandes over shortest paths), the computation of
  * run_bc (btwcentral/csr_bc.c:16-64) on a resident graph instead of a file:
  * for every source s (sources[0..k), or every vertex when sources is NULL)

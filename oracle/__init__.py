@@ -66,6 +66,8 @@ def lib() -> ctypes.CDLL:
         for name in ("or_delta_stepping_u32", "or_delta_stepping_f32", "or_delta_stepping_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _dbl, _P, _P]
             getattr(L, name).restype = ctypes.c_int
+        L.or_pagerank.argtypes = [_u32, _P, _P, ctypes.c_double, ctypes.c_double, _u32, _P]
+        L.or_pagerank.restype = ctypes.c_int
         for name in ("or_bc_u32", "or_bc_f32", "or_bc_f64"):
             getattr(L, name).argtypes = [_u32, _P, _P, _P, _u32, _P, _P]
             getattr(L, name).restype = ctypes.c_int
@@ -408,3 +410,31 @@ def read_bin(data: bytes, direction: int, target_offset: int = 1, dedup: bool = 
     row, col = _stable_csr(rows, cols, v_num)
     w = np.where(np.arange(len(col)) % 2 == 0, 0.1, 0.2)
     return row, col, w, hdr
+
+
+def pagerank(in_row, in_col, random_jump: float = 0.3, threshold: float = 1e-6, max_iters: int = 10000):
+    """The reference's PageRank iteration on an in-edge CSR (row v lists the
+    sources of the edges into v), restating pagerank/pagerank_mpi.c:667-1043
+    on one node.  Returns (rank float64[n], iterations)."""
+    row = np.ascontiguousarray(in_row, dtype=np.uint64)
+    col = np.ascontiguousarray(in_col, dtype=np.uint32)
+    n = len(row) - 1
+    out = np.empty(n, dtype=np.float64)
+    it = lib().or_pagerank(n, _ptr(row), _ptr(col), float(random_jump), float(threshold), int(max_iters), _ptr(out))
+    if it < 0:
+        raise RuntimeError("oracle pagerank failed")
+    return out, it
+
+
+def transpose(row, col):
+    """In-edge CSR of an out-edge CSR: row v of the result lists the u with an
+    edge u -> v, in the order the out-edge CSR lists them (by u, then
+    position)."""
+    row = np.asarray(row, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    n = len(row) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(row))
+    order = np.argsort(col, kind="stable")
+    t_row = np.zeros(n + 1, dtype=np.uint64)
+    np.add.at(t_row, col + 1, 1)
+    return np.cumsum(t_row).astype(np.uint64), src[order].astype(np.uint32)

@@ -617,3 +617,72 @@ int or_bc_f64(uint32_t n, const uint64_t *row, const uint32_t *col, const double
               const uint32_t *srcs, double *bc) {
     OR_BC_BODY(double, double, or_dijkstra_f64, or_tight_f64, OR_INF_FP)
 }
+
+/* ------------------------------------------------------------ PageRank */
+/* The reference's PageRank iteration (pagerank/pagerank_mpi.c:667-1043 on
+ * one node; constants RDM_JMP 0.3 and THRESH 1e-6, include/graph.h:17-18):
+ * weight[v] = 1 (init_weight, :64-68), recip[v] = 1 / out-degree(v) (the
+ * partitioner's recip files, partition/csr_partition_bin_mpi.c:227),
+ * wb[v] = rj, diff[v] = weight[v] * recip[v] (:752-754); every iteration
+ *   wb[v] += (1 - rj) * diff[u] over the in-edges u of v       (:879-890)
+ *   diff[v] = (wb[v] - weight[v]) * recip[v]                   (:995-997)
+ *   done unless some |diff[v]| > thresh; weight[v] = wb[v]      (:998-1002)
+ * row/col: the IN-edge CSR (row v lists the u with an edge u -> v).
+ * Summation order of the per-iteration increment of wb[v] (fixed here; the
+ * reference adds straight into wb[v] in row order): the row keeps its CSR
+ * positions, grouped in 32-position words; a word's terms are added from the
+ * lowest position up starting from 0; the row's words, numbered from its first
+ * word, form blocks of 32 whose word sums are combined by the butterfly
+ * (h = 16..1: s[i] += s[i + h]); the block sums are added in order from 0;
+ * wb[v] += that sum.  Returns the iterations taken (< 0 on error). */
+int or_pagerank(uint32_t n, const uint64_t *row, const uint32_t *col, double rj, double thresh,
+                uint32_t max_iters, double *weight_out) {
+    const double pj = 1.0 - rj;
+    double *weight = weight_out, *wb = (double *)malloc(8 * (size_t)n);
+    double *recip = (double *)malloc(8 * (size_t)n), *diff = (double *)malloc(8 * (size_t)n);
+    double *nd = (double *)malloc(8 * (size_t)n);
+    uint64_t *outdeg = (uint64_t *)calloc((size_t)n, 8);
+    if (!wb || !recip || !diff || !nd || !outdeg) return -1;
+    for (uint64_t e = 0; e < row[n]; e++) outdeg[col[e]]++;
+    for (uint32_t v = 0; v < n; v++) {
+        weight[v] = 1.0;
+        recip[v] = 1.0 / (double)outdeg[v];
+        wb[v] = rj;
+        diff[v] = weight[v] * recip[v];
+    }
+    uint32_t it = 0;
+    for (;;) {
+        it++;
+        int done = 1;
+        for (uint32_t v = 0; v < n; v++) {
+            double acc = 0.0;
+            if (row[v + 1] > row[v]) {
+                const uint64_t wb0 = row[v] / 32, nw = (row[v + 1] - 1) / 32 + 1 - wb0;
+                for (uint64_t b = 0; b * 32 < nw; b++) {
+                    double q[32];
+                    for (int j = 0; j < 32; j++) {
+                        q[j] = 0.0;
+                        if (b * 32 + j >= nw) continue;
+                        const uint64_t W = wb0 + b * 32 + j;
+                        const uint64_t lo = W * 32 > row[v] ? W * 32 : row[v];
+                        const uint64_t hi = W * 32 + 32 < row[v + 1] ? W * 32 + 32 : row[v + 1];
+                        double p = 0.0;
+                        for (uint64_t e = lo; e < hi; e++) p += pj * diff[col[e]];
+                        q[j] = p;
+                    }
+                    acc += or_butterfly32(q);
+                }
+            }
+            wb[v] += acc;
+            nd[v] = (wb[v] - weight[v]) * recip[v];
+        }
+        for (uint32_t v = 0; v < n; v++) {
+            if (fabs(nd[v]) > thresh) done = 0;
+            weight[v] = wb[v];
+            diff[v] = nd[v];
+        }
+        if (done || it >= max_iters) break;
+    }
+    free(wb); free(recip); free(diff); free(nd); free(outdeg);
+    return (int)it;
+}
