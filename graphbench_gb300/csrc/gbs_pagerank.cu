@@ -43,8 +43,10 @@ struct PrArgs {
     double thresh;
     const double *recip;
     double *weight, *wb;
-    const double *diff;     // this iteration's input
-    double *diff_next;      // its output
+    const double *diff;     // this iteration's input, times (1 - rj)
+    double *diff_next;      // its output, times (1 - rj)
+    const uint32_t *srow;    // the rows of at most kShort edges, grouped by degree
+    uint32_t n_short;
     const uint32_t *lw_row;  // words of the long rows: row, mask word
     const uint32_t *lw_w;
     uint32_t n_lw;
@@ -62,6 +64,8 @@ __global__ void k_outdeg(const uint32_t *__restrict__ col, unsigned long long m,
         atomicAdd(deg + col[e], 1u);
 }
 
+// diff is kept multiplied by (1 - rj): every edge term (1 - rj) * diff[u] is
+// then a load, the same product computed once per vertex instead of per edge.
 __global__ void k_pr_init(const uint32_t *__restrict__ deg, uint32_t n, double rj, double *__restrict__ recip,
                           double *__restrict__ weight, double *__restrict__ wb, double *__restrict__ diff) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -69,7 +73,7 @@ __global__ void k_pr_init(const uint32_t *__restrict__ deg, uint32_t n, double r
         recip[v] = r;
         weight[v] = 1.0;
         wb[v] = rj;
-        diff[v] = __dmul_rn(1.0, r);
+        diff[v] = __dmul_rn(1.0 - rj, __dmul_rn(1.0, r));
     }
 }
 
@@ -78,26 +82,47 @@ __device__ __forceinline__ void pr_update(const PrArgs &a, uint32_t v, double s)
     const double d = __dmul_rn(__dadd_rn(w, -a.weight[v]), a.recip[v]);
     a.wb[v] = w;
     a.weight[v] = w;
-    a.diff_next[v] = d;
+    a.diff_next[v] = __dmul_rn(a.pj, d);
     if (fabs(d) > a.thresh) *a.flag = 1u;   // NaN compares false, as in the reference
+}
+
+// Positions [lo, hi) of one row added in order into p (acc takes p at each
+// change of 32-position word); 8 gathers in flight before their adds.
+constexpr int kPull = 8;
+__device__ __forceinline__ void pull_range(const PrArgs &a, unsigned long long lo, unsigned long long hi, double &acc,
+                                           double &p, unsigned long long &cur) {
+    for (unsigned long long e0 = lo; e0 < hi; e0 += kPull) {
+        uint32_t u[kPull];
+        double t[kPull];
+#pragma unroll
+        for (int k = 0; k < kPull; ++k) u[k] = e0 + k < hi ? __ldg(a.col + e0 + k) : 0u;
+#pragma unroll
+        for (int k = 0; k < kPull; ++k) t[k] = e0 + k < hi ? __ldg(a.diff + u[k]) : 0.0;
+#pragma unroll
+        for (int k = 0; k < kPull; ++k) {
+            const unsigned long long e = e0 + k;
+            if (e < hi) {
+                if ((e >> 5) != cur) {
+                    acc = __dadd_rn(acc, p);
+                    p = 0.0;
+                    cur = e >> 5;
+                }
+                p = __dadd_rn(p, t[k]);
+            }
+        }
+    }
 }
 
 // Short rows summed by their thread; word sums of the long rows.
 __global__ void __launch_bounds__(256) k_pr_pull(PrArgs a) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += stride) {
+    // a warp's rows have equal degrees, so its FP64 adds run with every lane busy
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_short; i += stride) {
+        const uint32_t v = a.srow[i];
         const unsigned long long beg = a.row[v], end = a.row[v + 1];
-        if (end - beg > kShort) continue;
         double acc = 0.0, p = 0.0;
         unsigned long long cur = beg >> 5;
-        for (unsigned long long e = beg; e < end; ++e) {
-            if ((e >> 5) != cur) {
-                acc = __dadd_rn(acc, p);
-                p = 0.0;
-                cur = e >> 5;
-            }
-            p = __dadd_rn(p, __dmul_rn(a.pj, __ldg(a.diff + __ldg(a.col + e))));
-        }
+        pull_range(a, beg, end, acc, p, cur);
         acc = __dadd_rn(acc, p);
         pr_update(a, v, acc);
     }
@@ -106,8 +131,9 @@ __global__ void __launch_bounds__(256) k_pr_pull(PrArgs a) {
         const unsigned long long W = a.lw_w[x];
         const unsigned long long beg = a.row[v], end = a.row[v + 1];
         const unsigned long long lo = max(beg, W << 5), hi = min(end, (W << 5) + 32ull);
-        double p = 0.0;
-        for (unsigned long long e = lo; e < hi; ++e) p = __dadd_rn(p, __dmul_rn(a.pj, __ldg(a.diff + __ldg(a.col + e))));
+        double acc = 0.0, p = 0.0;
+        unsigned long long cur = W;
+        pull_range(a, lo, hi, acc, p, cur);
         a.part[x] = p;
     }
 }
@@ -225,9 +251,17 @@ gbs_status run_pagerank(const gbs_device_csr *c, const gbs_pagerank_params *para
     std::vector<unsigned long long> row(n + 1ull);
     GBS_CUDA(cudaMemcpy(row.data(), c->d_row, sizeof(unsigned long long) * (n + 1ull), cudaMemcpyDeviceToHost));
     std::vector<uint32_t> lw_row, lw_w, lr_row, lr_first, lr_nw;
+    std::vector<uint32_t> short_cnt(kShort + 2, 0), srow;
+    for (uint32_t v = 0; v < n; ++v)
+        if (row[v + 1] - row[v] <= kShort) ++short_cnt[row[v + 1] - row[v] + 1];
+    for (uint32_t d = 1; d < kShort + 2; ++d) short_cnt[d] += short_cnt[d - 1];
+    srow.resize(short_cnt[kShort + 1]);
     for (uint32_t v = 0; v < n; ++v) {
         const unsigned long long beg = row[v], end = row[v + 1];
-        if (end - beg <= kShort) continue;
+        if (end - beg <= kShort) {
+            srow[short_cnt[end - beg]++] = v;
+            continue;
+        }
         const unsigned long long wb = beg >> 5, we = (end >> 5) + ((end & 31ull) != 0ull);
         lr_row.push_back(v);
         lr_first.push_back((uint32_t)lw_row.size());
@@ -255,6 +289,7 @@ gbs_status run_pagerank(const gbs_device_csr *c, const gbs_pagerank_params *para
     } ef{e0, e1};
     Pool pool;
     uint32_t *deg = nullptr, *flag = nullptr, *lwr = nullptr, *lww = nullptr, *lrr = nullptr, *lrf = nullptr, *lrn = nullptr;
+    uint32_t *srw = nullptr;
     double *recip = nullptr, *weight = nullptr, *wb = nullptr, *diff[2] = {nullptr, nullptr}, *part = nullptr;
     GBS_CUDA(pool.get(&deg, n));
     GBS_CUDA(pool.get(&flag, 1));
@@ -269,6 +304,8 @@ gbs_status run_pagerank(const gbs_device_csr *c, const gbs_pagerank_params *para
     GBS_CUDA(pool.get(&lrr, lr_row.size()));
     GBS_CUDA(pool.get(&lrf, lr_first.size()));
     GBS_CUDA(pool.get(&lrn, lr_nw.size()));
+    GBS_CUDA(pool.get(&srw, srow.size()));
+    if (!srow.empty()) GBS_CUDA(cudaMemcpyAsync(srw, srow.data(), 4 * srow.size(), cudaMemcpyHostToDevice, s));
     if (!lw_row.empty()) {
         GBS_CUDA(cudaMemcpyAsync(lwr, lw_row.data(), 4 * lw_row.size(), cudaMemcpyHostToDevice, s));
         GBS_CUDA(cudaMemcpyAsync(lww, lw_w.data(), 4 * lw_w.size(), cudaMemcpyHostToDevice, s));
@@ -290,6 +327,8 @@ gbs_status run_pagerank(const gbs_device_csr *c, const gbs_pagerank_params *para
     a.recip = recip;
     a.weight = weight;
     a.wb = wb;
+    a.srow = srw;
+    a.n_short = (uint32_t)srow.size();
     a.lw_row = lwr;
     a.lw_w = lww;
     a.n_lw = (uint32_t)lw_row.size();
@@ -299,7 +338,7 @@ gbs_status run_pagerank(const gbs_device_csr *c, const gbs_pagerank_params *para
     a.lr_nw = lrn;
     a.n_lr = (uint32_t)lr_row.size();
     a.flag = flag;
-    const int g1 = grid_of(std::max<unsigned long long>(n, lw_row.size()), sms);
+    const int g1 = grid_of(std::max<unsigned long long>(srow.size(), lw_row.size()), sms);
     const int g2 = std::max(1, std::min<int>((int)((lr_row.size() + 255) / 256), sms * 16));
     uint32_t it = 0, more = 1;
     while (more && it < max_iters) {
