@@ -62,7 +62,7 @@ class Params(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
                 ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
                 ("solo_entries", ctypes.c_uint32), ("solo_descs", ctypes.c_uint32),
-                ("inline_edges", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("inline_edges", ctypes.c_uint32), ("full_items", ctypes.c_uint32)]
 
 
 class PhaseRec(ctypes.Structure):
@@ -456,7 +456,7 @@ class Graph:
     @staticmethod
     def params(delta: float | None = None, light: float | None = None, flags: int = 0,
                wait_limit_ms: int = 0, solo_entries: int = 0, solo_descs: int = 0,
-               inline_edges: int = 0) -> Params:
+               inline_edges: int = 0, full_items: int = 0) -> Params:
         p = Params()
         p.delta = float(delta) if delta else 0.0
         p.light = float(light) if light is not None else -1.0
@@ -465,6 +465,7 @@ class Graph:
         p.solo_entries = solo_entries
         p.solo_descs = solo_descs
         p.inline_edges = inline_edges
+        p.full_items = full_items
         return p
 
     def trace(self) -> list[dict]:

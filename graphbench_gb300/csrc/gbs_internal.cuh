@@ -201,6 +201,8 @@ struct SsspArgs {
     uint32_t solo_desc;     // an EDGES phase with at most this many descriptors runs on one CTA
     uint32_t no_heavy;      // the split covers every edge: light scans relax whole rows, no HEAVY phase
     uint32_t inline_max;    // rows up to this long are relaxed by the scanning warp
+    uint32_t full_items;    // kCtrlFixed: a bucket whose lists hold at most this many entries when it
+                            // starts relaxes whole rows (no heavy phase)
     // bucket-width controller
     uint32_t ctrl;          // CtrlMode
     uint32_t span_fixed;    // kCtrlFixed: base widths per bucket (0 or 1 = plain delta-stepping)

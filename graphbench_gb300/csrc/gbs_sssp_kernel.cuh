@@ -54,6 +54,7 @@ enum Phase : uint32_t {
 constexpr int kUnroll = 4;
 constexpr uint32_t kDescEdges = 32u * kUnroll;   // edges per descriptor (one warp round)
 constexpr uint32_t kInlineEdges = 32u;           // default inline_max: rows up to this long are relaxed in SCAN
+constexpr uint32_t kFullItems = 1024u;           // default full_items: smaller buckets relax whole rows
 
 // Values identical in every CTA (the kernel's uniform state).
 struct Uniform {

@@ -501,6 +501,10 @@ __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint3
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(FULL, cnt, o);
     first_items = cnt;
+    // a bucket that starts this small relaxes whole rows: its heavy phase
+    // would cost a grid step for a handful of edges (distances are the same
+    // least fixpoint either way)
+    if (a.ctrl == kCtrlFixed && cnt <= a.full_items) full_out = 1u;
 }
 
 // The uniform state after the decision (identical in every CTA that adopts it).

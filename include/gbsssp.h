@@ -78,7 +78,9 @@ typedef struct gbs_params {
     uint32_t inline_edges;   /* rows of at most this many edges are relaxed by the
                                 scanning warp, longer rows are cut into 128-edge
                                 descriptors relaxed one warp each; 0 = 32 */
-    uint32_t reserved;
+    uint32_t full_items;     /* a bucket whose lists hold at most this many entries
+                                when it starts relaxes whole rows (light and heavy
+                                edges together, no heavy phase); 0 = 1024 */
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
