@@ -27,6 +27,9 @@ Each reports GTEPS and its ratio to the plain value.
   betweenness  gbs_bc over 16 of the sources (batched shortest paths, then
              the path-count / dependency passes per source), with a bit-exact
              check of one more source against the oracle at full scale
+  pagerank   gbs_pagerank on the same graph (in-edges), to convergence
+  ingest     the same edges as a shuffled binary edge list parsed on the GPU
+             with duplicate removal, CSR and resident graph built there
 
 Multi-GPU: one process per GPU (torchrun); every rank runs the whole workload
 on its own GPU (replicas: a single SSSP does not shard); value = sum over
@@ -290,6 +293,68 @@ def arm_betweenness(gb, g, hg, srcs, cpu: bool, n_src: int = 16):
     return out
 
 
+def arm_pagerank(gb, hg, cpu: bool):
+    """PageRank (gbs_pagerank) on the workload's graph as in-edges (the graph
+    is symmetric), from a device CSR built by the ingest path; the oracle's
+    restatement on R-MAT 18 is the CPU baseline."""
+    with gb.DeviceCsr.from_arrays(hg.row, hg.col) as c, c.transpose() as t:
+        t.pagerank(max_iters=2)
+        _, st = t.pagerank()
+    out = {"value": st["edges"] * st["iterations"] / st["device_ms"] / 1e6, "unit": "G edge-updates/s",
+           "iterations": st["iterations"], "converged": st["converged"], "ms": st["device_ms"],
+           "ms_per_iteration": st["device_ms"] / max(st["iterations"], 1),
+           "path": "gbs_device_csr_transpose + gbs_pagerank (RDM_JMP 0.3, THRESH 1e-6, float64)"}
+    if cpu:
+        import oracle
+        from oracle import gen
+        row, col, _ = gen.rmat(18, 16, 1, "u32")
+        tr, tc = oracle.transpose(row, col)
+        t0 = time.perf_counter()
+        _, it = oracle.pagerank(tr, tc)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": int(row[-1]) * it / secs / 1e9, "unit": "G edge-updates/s", "cores": 1,
+                               "kind": "port", "sample": f"R-MAT 18, {it} iterations, oracle or_pagerank, {secs:.1f} s"}
+    return out
+
+
+def arm_ingest(gb, hg, cpu: bool):
+    """The binary edge-list reader (gbs_parse_bin: read_csr_bin's layout, with
+    duplicate removal) and the device build of the resident graph, on the
+    workload's edges in shuffled file order, from host memory."""
+    n, m = hg.n, hg.m
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(hg.row.astype(np.int64)))
+    perm = np.random.default_rng(1).permutation(m)
+    pairs = np.empty((m, 2), dtype="<i8")
+    pairs[:, 0] = src[perm] + 1
+    pairs[:, 1] = hg.col.astype(np.int64)[perm] + 1
+    data = np.array([n, m, 1, n], dtype="<i8").tobytes() + pairs.tobytes()
+    del pairs, src, perm
+    with gb.DeviceCsr.parse_bin(data, gb.DIR_SEND, 1, True):
+        pass
+    with gb.DeviceCsr.parse_bin(data, gb.DIR_SEND, 1, True) as c:
+        info = dict(c.info)
+        t0 = time.perf_counter()
+        g = c.graph(gb.W_F64)
+        gb.synchronize()
+        graph_ms = (time.perf_counter() - t0) * 1e3
+        g.close()
+    dev_ms = info["parse_ms"] + info["build_ms"]
+    out = {"value": len(data) / dev_ms / 1e6, "unit": "GB/s of file parsed and built (device)",
+           "bytes": len(data), "pairs": m, "duplicates": info["duplicates"], "parse_ms": info["parse_ms"],
+           "build_ms": info["build_ms"], "resident_graph_ms": graph_ms,
+           "path": "gbs_parse_bin (dedup) + gbs_graph_from_device_csr; bytes in pinned-less host memory"}
+    if cpu:
+        import oracle
+        k = min(m, 8_000_000)
+        sample = np.array([n, k, 1, n], dtype="<i8").tobytes() + data[32:32 + 16 * k]
+        t0 = time.perf_counter()
+        oracle.read_bin(sample, 1, 1, False)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(sample) / secs / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                               "sample": f"first {k} pairs, oracle read_bin (numpy), {secs:.1f} s"}
+    return out
+
+
 # ----------------------------------------------------------------- our arm
 def run_ours(args):
     world, rank, local = dist_env()
@@ -418,6 +483,14 @@ def run_ours(args):
             except Exception as e:  # pragma: no cover
                 result["betweenness"] = {"value": None, "error": str(e)}
             log(f"[rank 0] betweenness: {result['betweenness'].get('value')}")
+        if world == 1 and not args.no_bc:
+            for name, fn in (("pagerank", lambda: arm_pagerank(gb, hg, not args.no_cpu_baseline)),
+                             ("ingest", lambda: arm_ingest(gb, hg, not args.no_cpu_baseline))):
+                try:
+                    result[name] = fn()
+                except Exception as e:  # pragma: no cover
+                    result[name] = {"value": None, "error": str(e)}
+                log(f"[rank 0] {name}: {result[name].get('value')}")
         if world == 1 and not args.no_cpu_baseline:
             try:
                 result["cpu_baseline"] = cpu_baseline_port(hg, srcs, st0["delta_used"], args.cpu_budget_s)
@@ -529,7 +602,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-arms", action="store_true", help="skip the learned / autotuned / batched arms")
-    ap.add_argument("--no-bc", action="store_true", help="skip the betweenness measurement")
+    ap.add_argument("--no-bc", action="store_true", help="skip the betweenness, PageRank and ingest measurements")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-scale", type=int, default=16)
     ap.add_argument("--ref-procs", type=int, default=16)
