@@ -246,7 +246,7 @@ def arm_autotuned(gb, g, order, W, K, srcs):
 
 def arm_batched(gb, g, srcs, reps: int = 5):
     t0 = time.time()
-    bp, rep = gb.autotune_plan(g, srcs, budget_ms=4000)
+    bp, rep = gb.autotune_plan(g, srcs, budget_ms=8000)
     tune_s = time.time() - t0
     with gb.Plan(g, srcs, params=bp) as plan:
         for _ in range(2):

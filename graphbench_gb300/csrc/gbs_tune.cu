@@ -5,6 +5,7 @@
 // alone; batched: the graph launch).  The result of any schedule is the same
 // least fixpoint, so the search only compares times.
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -151,40 +152,52 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
 
 namespace {
 
-// Creates a plan without outputs, runs it once untimed and once timed.
+// Creates a plan without outputs and runs it once; a run within `close_ms`
+// is repeated and the faster of the two counts (a clear loser costs one run).
 template <class Make>
-gbs_status time_plan(Make make, const gbs_batch_params &bp, Budget &b, double &ms) {
+gbs_status time_plan(Make make, const gbs_batch_params &bp, Budget &b, double close_ms, double &ms) {
     gbs_plan *plan = nullptr;
     gbs_status s = make(bp, &plan);
     if (s != GBS_OK) return s;
     gbs_batch_stats st;
-    for (int rep = 0; rep < 2 && s == GBS_OK; ++rep) {
+    ms = INFINITY;
+    for (int rep = 0; rep < 2; ++rep) {
         s = gbs_plan_launch(plan);
         if (s == GBS_OK) s = gbs_plan_wait(plan, &st, nullptr);
-        if (s == GBS_OK) b.used_ms += st.device_ms;
+        if (s != GBS_OK) break;
+        b.used_ms += st.device_ms;
+        ms = std::min(ms, (double)st.device_ms);
+        if (ms > close_ms) break;
     }
     gbs_plan_destroy(plan);
-    ms = st.device_ms;
     return s;
 }
 
+// Search order: the seed schedule (when given) against the default at the
+// automatic group shape; the group shape at the better of the two; the bucket
+// width and split at the best shape (around the seed's width, or coarse
+// exponents of the default width without a seed, then the neighbours of the
+// best); the shapes next to the best one at the best schedule; the inline-row
+// limit.  A candidate whose first run is 1.1x slower than the best so far is
+// not run again.
 template <class Make>
-gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, gbs_batch_tune_report *out) {
-    Budget b{budget_ms > 0 ? budget_ms : 4000.0};
+gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, const gbs_batch_params *seed,
+                     gbs_batch_tune_report *out) {
+    Budget b{budget_ms};
     std::memset(out, 0, sizeof(*out));
     gbs_batch_params base{};
     base.light = -1.0;
     double ms = 0.0;
-    gbs_status s = time_plan(make, base, b, ms);
+    gbs_status s = time_plan(make, base, b, INFINITY, ms);
     if (s != GBS_OK) return s;
     out->default_ms = ms;
     out->candidates = 1;
     gbs_batch_params best = base;
     double best_ms = ms;
-    auto consider = [&](const gbs_batch_params &p) -> gbs_status {
+    auto consider = [&](const gbs_batch_params &p, double &t) -> gbs_status {
+        t = INFINITY;
         if (!b.left()) return GBS_OK;
-        double t = 0.0;
-        gbs_status r = time_plan(make, p, b, t);
+        gbs_status r = time_plan(make, p, b, 1.1 * best_ms, t);
         if (r == GBS_ERR_NO_MEMORY) return GBS_OK;   // a shape that does not fit is skipped
         if (r != GBS_OK) return r;
         ++out->candidates;
@@ -194,32 +207,91 @@ gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, gbs_batch
         }
         return GBS_OK;
     };
-    // 1. CTAs per group (powers of two and the divisors of the SM count)
+    // width exponents e (delta_scale 2^e) for both splits around `shape`
+    auto width_search = [&](const gbs_batch_params shape, const int *coarse, size_t n_coarse) -> gbs_status {
+        for (int split = 0; split < 2; ++split) {
+            std::vector<std::pair<int, double>> seen;
+            auto eval = [&](int e) -> gbs_status {
+                if (e < kMinExp || e > kMaxExp) return GBS_OK;
+                for (auto &q : seen)
+                    if (q.first == e) return GBS_OK;
+                gbs_batch_params p = shape;
+                p.delta_scale = std::ldexp(1.0, e);
+                p.light = split ? INFINITY : -1.0;
+                double t = 0.0;
+                gbs_status r;
+                const bool same = std::memcmp(&p, &best, sizeof(p)) == 0 ||
+                                  (p.delta_scale == 1.0 && split == 0 && shape.delta_scale <= 0 &&
+                                   shape.light < 0 && std::memcmp(&shape, &best, sizeof(p)) == 0);
+                if (same) {
+                    t = best_ms;
+                } else if ((r = consider(p, t)) != GBS_OK) {
+                    return r;
+                }
+                seen.push_back({e, t});
+                return GBS_OK;
+            };
+            for (size_t i = 0; i < n_coarse; ++i)
+                if ((s = eval(coarse[i])) != GBS_OK) return s;
+            for (int round = 0; round < 2 && !seen.empty(); ++round) {
+                int be = seen[0].first;
+                double bm = seen[0].second;
+                for (auto &q : seen)
+                    if (q.second < bm) {
+                        bm = q.second;
+                        be = q.first;
+                    }
+                for (int d : {-1, 1})
+                    if ((s = eval(be + d)) != GBS_OK) return s;
+            }
+        }
+        return GBS_OK;
+    };
+    // 0. the seed
+    if (seed) {
+        double t;
+        if ((s = consider(*seed, t)) != GBS_OK) return s;
+    }
+    // 1. CTAs per group (powers of two and the divisors of the SM count),
+    //    widest first
     std::vector<uint32_t> shapes;
     for (uint32_t gc = 1; gc <= max_blocks; gc *= 2) shapes.push_back(gc);
     for (uint32_t d = 3; d <= max_blocks; ++d)
         if (max_blocks % d == 0 && (d & (d - 1)) != 0) shapes.push_back(d);
-    std::sort(shapes.begin(), shapes.end());
+    std::sort(shapes.begin(), shapes.end(), std::greater<uint32_t>());
+    const gbs_batch_params sched0 = best;
     for (uint32_t gc : shapes) {
-        gbs_batch_params p = base;
+        gbs_batch_params p = sched0;
         p.group_ctas = gc;
-        if ((s = consider(p)) != GBS_OK) return s;
+        double t;
+        if ((s = consider(p, t)) != GBS_OK) return s;
     }
     // 2. schedule at the best shape
-    const gbs_batch_params shape = best;
-    for (int split = 0; split < 2; ++split) {
-        for (double sc : {0.5, 1.0, 2.0, 4.0, 8.0, 16.0}) {
-            if (split == 0 && sc == 1.0) continue;
-            gbs_batch_params p = shape;
-            p.delta_scale = sc;
-            p.light = split ? INFINITY : -1.0;
-            if ((s = consider(p)) != GBS_OK) return s;
+    if (seed) {
+        const int e0 = seed->delta_scale > 0 ? (int)std::lround(std::log2(seed->delta_scale)) : 0;
+        if ((s = width_search(best, &e0, 1)) != GBS_OK) return s;
+    } else if ((s = width_search(best, kCoarse, sizeof(kCoarse) / sizeof(kCoarse[0]))) != GBS_OK) {
+        return s;
+    }
+    // 3. the shapes next to the best one, at the best schedule
+    if (best.group_ctas != 0) {
+        const gbs_batch_params sched = best;
+        const auto it = std::find(shapes.begin(), shapes.end(), sched.group_ctas);
+        const size_t k = (size_t)(it - shapes.begin());
+        for (size_t j : {k - 1, k + 1}) {
+            if (it == shapes.end() || j >= shapes.size()) continue;
+            gbs_batch_params p = sched;
+            p.group_ctas = shapes[j];
+            double t;
+            if ((s = consider(p, t)) != GBS_OK) return s;
         }
     }
+    // 4. inline-row limit
     for (uint32_t v : kInline) {
         gbs_batch_params p = best;
         p.inline_edges = v;
-        if ((s = consider(p)) != GBS_OK) return s;
+        double t;
+        if ((s = consider(p, t)) != GBS_OK) return s;
     }
     out->best = best;
     out->best_ms = best_ms;
@@ -239,10 +311,24 @@ extern "C" {
 gbs_status gbs_autotune_plan_sources(gbs_graph *g, const uint32_t *sources, uint32_t k, double budget_ms,
                                      gbs_batch_tune_report *out) {
     if (!g || !sources || k == 0 || !out) return fail(GBS_ERR_INVALID_ARG, "graph, sources and out are required");
+    for (uint32_t i = 0; i < k; ++i)
+        if (sources[i] >= g->n) return fail(GBS_ERR_INVALID_ARG, "source out of range");
     auto make = [&](const gbs_batch_params &bp, gbs_plan **plan) {
         return gbs_plan_sources(g, sources, k, &bp, nullptr, nullptr, plan);
     };
-    return tune_plan(make, batch_blocks(g->device), budget_ms, out);
+    // seed: the single-source tuner on (up to) two of the sources, with a
+    // third of the budget; its width, split and knobs carry over to groups
+    const double total = budget_ms > 0 ? budget_ms : 8000.0;
+    gbs_tune_report sr;
+    gbs_status s = gbs_autotune(g, sources, std::min(k, 2u), total / 3.0, &sr);
+    if (s != GBS_OK) return s;
+    gbs_batch_params seed{};
+    seed.delta_scale = sr.delta_scale;
+    seed.light = sr.no_split ? INFINITY : -1.0;
+    seed.solo_entries = sr.best.solo_entries;
+    seed.solo_descs = sr.best.solo_descs;
+    seed.inline_edges = sr.best.inline_edges;
+    return tune_plan(make, batch_blocks(g->device), total * 2.0 / 3.0, &seed, out);
 }
 
 gbs_status gbs_autotune_plan_pack(gbs_pack *pk, const uint32_t *sources, double budget_ms,
@@ -253,7 +339,7 @@ gbs_status gbs_autotune_plan_pack(gbs_pack *pk, const uint32_t *sources, double 
     auto make = [&](const gbs_batch_params &bp, gbs_plan **plan) {
         return gbs_plan_pack(pk, sources, &bp, nullptr, nullptr, plan);
     };
-    return tune_plan(make, batch_blocks(dev), budget_ms, out);
+    return tune_plan(make, batch_blocks(dev), budget_ms > 0 ? budget_ms : 4000.0, nullptr, out);
 }
 
 }  // extern "C"
