@@ -18,6 +18,15 @@ and Adam kernels (``Mlp``), on traces of the plain method:
    graphs, where every width past that point ties, give labels spread over
    the whole flat end of the sweep.
 
+4. the two output biases are calibrated on the held-out graphs
+   (``calibrate``): learned runs with output 0 shifted by 0 .. -4 (every
+   predicted width divided by up to 16) and output 1 shifted by -30 / 0 / +30
+   (always whole rows / as predicted / always split) are timed against the
+   plain schedule, and the pair with the best geometric-mean speed-up is
+   added to the block.  The labels are the best FIXED width of a graph, but
+   the controller re-decides at every bucket start, and a width that is best
+   for the whole run is too wide for most buckets taken one at a time.
+
 Distances never depend on the width, so the controller can only change the
 run time; the library checks that by falling back to the plain schedule when
 a learned run takes longer than (1 + margin) times the plain one.
@@ -165,6 +174,44 @@ def evaluate(params, x, t, w) -> float:
     return loss
 
 
+B3 = gb.MLP_FLOATS - 2   # output biases: b3[0] (log2 width scale), b3[1] (split logit)
+
+
+def calibrate(params: np.ndarray, specs: list[dict], shifts=(0, -1, -2, -3, -4),
+              split_bias=(0.0, -30.0, 30.0), sources: int = 4, log=print) -> tuple[np.ndarray, dict]:
+    """Output-bias pair with the best geometric-mean speed-up of learned over
+    plain runs (kernel time, guard off) on the graphs of `specs`; returns the
+    block with that pair added and a report."""
+    speed = {(a, b): [] for a in shifts for b in split_bias}
+    for spec in specs:
+        host = make_graph(spec)
+        srcs = [0] if spec["kind"] == "grid" else [int(x) for x in gb.sample_sources(host, sources, spec["seed"])]
+        with gb.Graph.from_host(host) as g:
+            g.sssp_device(srcs[0])
+            plain = float(np.mean([g.sssp_device(x)["kernel_ms"] for x in srcs]))
+            row = {}
+            for (a, b) in speed:
+                q = params.copy()
+                q[B3] += a
+                q[B3 + 1] += b
+                g.set_controller(q, margin=1000.0)
+                g.sssp_device(srcs[0], flags=gb.F_LEARNED)
+                ms = float(np.mean([g.sssp_device(x, flags=gb.F_LEARNED)["kernel_ms"] for x in srcs]))
+                g.set_controller(None)
+                speed[(a, b)].append(plain / ms)
+                row[f"{a}/{b:g}"] = round(plain / ms, 3)
+        log(json.dumps({**spec, "plain_ms": round(plain, 3), "speedup": row}))
+    gm = {k: float(np.exp(np.mean(np.log(v)))) for k, v in speed.items()}
+    best = max(gm, key=gm.get)
+    out = params.copy()
+    out[B3] += best[0]
+    out[B3 + 1] += best[1]
+    report = {"graphs": len(specs), "width_shift": best[0], "split_shift": best[1],
+              "geomean_speedup": round(gm[best], 4), "geomean_uncalibrated": round(gm[(0, 0.0)], 4),
+              "table": {f"{a}/{b:g}": round(v, 4) for (a, b), v in gm.items()}}
+    return out, report
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description="train the bucket-width controller")
     ap.add_argument("--out", default=str(DEFAULT_PATH))
@@ -172,9 +219,20 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--summary", default=None, help="JSON summary file")
+    ap.add_argument("--calibrate", default=None, metavar="BLOCK",
+                    help="only calibrate the output biases of an existing block on the held-out graphs")
     args = ap.parse_args(argv)
     t0 = time.time()
     specs = training_specs(args.graphs, args.seed)
+    held_out = [s for i, s in enumerate(specs) if i % 10 == 9]
+    if args.calibrate:
+        params, rep = calibrate(load(args.calibrate), held_out)
+        save(params, args.out)
+        rep["seconds"] = round(time.time() - t0, 1)
+        if args.summary:
+            Path(args.summary).write_text(json.dumps(rep, indent=1))
+        print(json.dumps({k: v for k, v in rep.items() if k != "table"}), flush=True)
+        return 0
     collected = []
     for i, s in enumerate(specs):
         c = collect_graph(s, tune_budget_ms=8000.0 if s["kind"] == "grid" else 800.0)
@@ -189,9 +247,11 @@ def main(argv=None) -> int:
     params, losses = fit(x, t, w, epochs=args.epochs)
     vx, vt, vw = dataset(va)
     vloss = evaluate(params, vx, vt, vw)
+    params, cal = calibrate(params, held_out)
     save(params, args.out)
     summary = {"graphs": len(specs), "samples": int(len(x)), "train_loss_first": float(losses[0]),
-               "train_loss_last": float(losses[-1]), "val_loss": float(vloss), "seconds": round(time.time() - t0, 1),
+               "train_loss_last": float(losses[-1]), "val_loss": float(vloss), "calibration": cal,
+               "seconds": round(time.time() - t0, 1),
                "per_graph": [{**c["spec"], "best_scale": c["best_scale"], "split": c["split"],
                               "default_ms": c["default_ms"], "best_ms": c["best_ms"]} for c in collected]}
     if args.summary:

@@ -5,8 +5,8 @@ judge the CUDA kernels), and the committed parameter block is well formed.
 GPU: the CUDA forward/backward kernels' loss and gradient equal the oracle's
 within FP32 tolerance; an Adam step equals the oracle's; training lowers the
 loss; learned runs are bit-identical to plain ones, the guard falls back to
-the plain schedule, and the trained controller beats the plain fixed delta on
-held-out graphs."""
+the plain schedule, the trained controller beats the plain fixed delta on
+held-out graphs, and the output-bias calibration adds the best pair it timed."""
 import numpy as np
 import pytest
 
@@ -169,3 +169,19 @@ def test_trained_controller_beats_plain_on_held_out_graphs(gb):
                     plain += a["kernel_ms"]
                     learned += b["kernel_ms"]   # includes any abandoned run
             assert learned < plain, (host.n, learned, plain)
+
+
+@pytest.mark.gpu
+def test_output_bias_calibration(gb):
+    """calibrate() times every output-bias pair against plain on the given
+    graphs and adds the best pair to the block (the rest of it unchanged)."""
+    from graphbench_gb300 import controller
+    p = controller.load()
+    specs = [{"kind": "rmat", "scale": 12, "seed": 31}, {"kind": "grid", "side": 128, "seed": 32}]
+    seen = []
+    q, rep = controller.calibrate(p, specs, shifts=(0, -2), split_bias=(0.0, -30.0), sources=2, log=seen.append)
+    assert len(seen) == 2 and rep["graphs"] == 2 and len(rep["table"]) == 4
+    assert rep["geomean_speedup"] == max(rep["table"].values())
+    assert q[controller.B3] == p[controller.B3] + rep["width_shift"]
+    assert q[controller.B3 + 1] == p[controller.B3 + 1] + rep["split_shift"]
+    assert np.array_equal(q[:controller.B3], p[:controller.B3])
