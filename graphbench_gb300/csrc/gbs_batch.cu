@@ -60,7 +60,7 @@ __global__ void k_batch_prep(const Workspace *__restrict__ ws, uint32_t groups, 
     for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
         Ctl *c = ws[g].ctl;
         c->bar_count = 0u;
-        c->bar_gen = 0u;
+        for (int i = 0; i < 8; ++i) c->pubw[i] = 0ull;
         c->error = 0u;
         c->trace_n = 0u;
     }

@@ -90,24 +90,20 @@ struct __align__(128) Line {
 struct __align__(128) Ctl {
     uint32_t bar_count;
     uint32_t pad0[31];
-    uint32_t bar_gen;
-    uint32_t pad1[31];
+    // the decision of each barrier, published in one line: word i holds
+    // (generation << 32) | field i (kPubWords fields, see PubField), so a
+    // waiting CTA's poll returns the state together with the release
+    unsigned long long pubw[8];
+    uint32_t pad1[16];
     uint32_t error;
     uint32_t trace_n;
-    // kernel state published by the deciding CTA at each barrier: the next
-    // phase and everything the CTAs need to run it
+    // state a launch starts from (set before the launch)
     uint32_t pub_phase;
-    uint32_t pub_logical;
     uint32_t pub_b;
-    uint32_t pub_W;
-    uint32_t pub_epoch;
-    uint32_t pub_hround;
-    uint32_t pub_pend_sel;
-    uint32_t pub_inst;            // instance being solved (batched launches)
-    uint32_t pub_span;            // base widths the current bucket spans
+    uint32_t pub_span;            // base widths bucket 0 spans
     uint32_t pub_full;            // 1: light scans relax whole rows, no heavy scan
     uint32_t feat_n;              // feature vectors recorded
-    uint32_t pad2[19];
+    uint32_t pad2[25];
     Line ring_cnt[kNB];
     Line fq_cnt[3];
     Line hdesc_cnt;
@@ -237,6 +233,14 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
     uint32_t v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;

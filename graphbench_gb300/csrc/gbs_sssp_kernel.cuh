@@ -68,6 +68,7 @@ struct Uniform {
     uint32_t inst;        // batched: instance being solved
     uint32_t span;        // base widths the current bucket spans (1..kNB)
     uint32_t full;        // 1: light scans relax whole rows and no heavy scan runs
+    uint32_t items;       // entries of the phase's input list (kNoItems: read the counters)
     uint32_t gen;         // barrier generation
     unsigned long long t0;  // globaltimer at kernel entry (per CTA)
 };

@@ -47,6 +47,17 @@ __device__ __forceinline__ Exec cta_exec() {
     return x;
 }
 
+// The decision of a barrier as published (Ctl::pubw): kPubWords fields, each
+// in the low half of a 64-bit word whose high half is the barrier generation.
+enum PubField : uint32_t { kPubState = 0, kPubB, kPubW, kPubEpoch, kPubHround, kPubInst, kPubItems, kPubWords };
+constexpr uint32_t kNoItems = 0xFFFFFFFFu;   // Uniform.items: not published, read the counters
+
+// phase | logical << 8 | pend_sel << 16 | full << 17 | span << 24 (span <= kNB)
+__device__ __forceinline__ uint32_t pack_state(const Uniform &N) {
+    return (N.phase & 0xFFu) | ((N.logical & 0xFFu) << 8) | ((N.pend_sel & 1u) << 16) | ((N.full & 1u) << 17) |
+           ((N.span & 0xFFu) << 24);
+}
+
 // ------------------------------------------------------------------- SCAN
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
@@ -235,10 +246,10 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exe
 // Moves pending vertices whose bucket entered the window [W, W+kNB) into the
 // ring; the rest go to the other pending list.
 template <int WT>
-__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr) {
+__device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
+                                 uint32_t count) {
     const uint32_t n = a.g.n;
     Ctl *ctl = a.ws.ctl;
-    const uint32_t count = min(__ldcg(&ctl->pend_cnt[U.pend_sel].v), n);
     const uint32_t *list = a.ws.pend + (size_t)U.pend_sel * n;
     Targets t;
     t.cur_hi = 0;
@@ -340,28 +351,33 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     t.pend_sel = U.pend_sel;
     t.scr = scr;
     const bool full = U.full != 0;
+    // the input size comes with the decision (U.items); the counters are
+    // read only where it was not published
+    const bool pub = U.items != kNoItems;
     switch (U.phase) {
         case kPhLightFirst:
             // the ring lists of every base bucket the bucket spans, one after
             // the other (independent: no barrier between them)
             for (uint32_t j = 0; j < U.span; ++j) {
                 const uint32_t bk = U.b + j;
-                scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n,
-                                  min(__ldcg(&ctl->ring_cnt[bk % kNB].v), n), bk, full, U.hround, imp);
+                const uint32_t c = (pub && U.span == 1u) ? U.items : __ldcg(&ctl->ring_cnt[bk % kNB].v);
+                scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n, min(c, n), bk, full, U.hround,
+                                  imp);
             }
             break;
         case kPhLight:
             scan_frontier<WT>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                              min(__ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, full, U.hround, imp);
+                              min(pub ? U.items : __ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, full,
+                              U.hround, imp);
             break;
         case kPhHeavy:
-            relax_heavy<WT>(a, t, x, min(__ldcg(&ctl->hdesc_cnt.v), a.ws.desc_cap), imp);
+            relax_heavy<WT>(a, t, x, min(pub ? U.items : __ldcg(&ctl->hdesc_cnt.v), a.ws.desc_cap), imp);
             break;
         case kPhEdges:
-            relax_descriptors<WT>(a, t, x, min(__ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
+            relax_descriptors<WT>(a, t, x, min(pub ? U.items : __ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
             break;
         case kPhPending:
-            rebucket_pending<WT>(a, U, x, scr);
+            rebucket_pending<WT>(a, U, x, scr, min(pub ? U.items : __ldcg(&ctl->pend_cnt[U.pend_sel].v), n));
             break;
         case kPhInit:
             init_instance(a, U, x);
@@ -528,12 +544,14 @@ __device__ __forceinline__ Uniform advance_uniform(const Uniform &U, uint32_t ne
 // Run by warp 0 of the deciding CTA after a phase: every other CTA has
 // finished it (or is waiting while this CTA runs alone), so all counters are
 // at rest.  Decides the next phase, resets the lists it appends to, records
-// statistics and the trace, publishes the new state and says whether the next
-// phase is small enough for this CTA to run alone.  In a batched launch the
+// statistics and the trace, writes the new state to s_pub (shared memory, in
+// the published layout) and says whether the next phase is small enough for
+// this CTA to run alone.  In a batched launch the
 // end of a run leads to FINISH, and after FINISH the group takes the next
 // instance from the queue (INIT) or stops.
 template <bool Batch>
-__device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool was_solo, bool &solo) {
+__device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool was_solo, bool &solo,
+                                    uint32_t *s_pub) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
@@ -728,16 +746,14 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             // last round's are relaxed, and at every new bucket
             if (U.phase == kPhHeavy || next == kPhLightFirst) ctl->hdesc_cnt.v = 0;
         }
-        ctl->pub_phase = N.phase;
-        ctl->pub_logical = N.logical;
-        ctl->pub_b = N.b;
-        ctl->pub_W = N.W;
-        ctl->pub_epoch = N.epoch;
-        ctl->pub_hround = N.hround;
-        ctl->pub_pend_sel = N.pend_sel;
-        ctl->pub_inst = N.inst;
-        ctl->pub_span = N.span;
-        ctl->pub_full = N.full;
+        // the decision, in the layout the release publishes
+        s_pub[kPubState] = pack_state(N);
+        s_pub[kPubB] = N.b;
+        s_pub[kPubW] = N.W;
+        s_pub[kPubEpoch] = N.epoch;
+        s_pub[kPubHround] = N.hround;
+        s_pub[kPubInst] = N.inst;
+        s_pub[kPubItems] = next < kPhDone ? items : kNoItems;
     }
     if (bucket_end) {   // the lists of the finished bucket
         if (lane < U.span) ctl->ring_cnt[(U.b + lane) % kNB].v = 0u;
@@ -773,46 +789,38 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     __syncwarp();
 }
 
-// Thread 0 copies the published state to shared memory; the caller syncs.
-__device__ __forceinline__ void fetch_published(Ctl *ctl, uint32_t *s_pub) {
-    const bool err = ld_relaxed(&ctl->error) != 0;
-    s_pub[0] = err ? (uint32_t)kPhDone : ld_relaxed(&ctl->pub_phase);
-    s_pub[1] = ld_relaxed(&ctl->pub_logical);
-    s_pub[2] = ld_relaxed(&ctl->pub_b);
-    s_pub[3] = ld_relaxed(&ctl->pub_W);
-    s_pub[4] = ld_relaxed(&ctl->pub_epoch);
-    s_pub[5] = ld_relaxed(&ctl->pub_hround);
-    s_pub[6] = ld_relaxed(&ctl->pub_pend_sel);
-    s_pub[7] = ld_relaxed(&ctl->pub_inst);
-    s_pub[8] = ld_relaxed(&ctl->pub_span);
-    s_pub[9] = ld_relaxed(&ctl->pub_full);
-}
-
+// The state of s_pub (published layout) as this CTA's uniform state.
 __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &U) {
-    U.phase = s_pub[0];
-    U.logical = s_pub[1];
-    U.b = s_pub[2];
-    U.W = s_pub[3];
-    U.epoch = s_pub[4];
-    U.hround = s_pub[5];
-    U.pend_sel = s_pub[6];
-    U.inst = s_pub[7];
-    U.span = s_pub[8];
-    U.full = s_pub[9];
+    const uint32_t st = s_pub[kPubState];
+    U.phase = st & 0xFFu;
+    U.logical = (st >> 8) & 0xFFu;
+    U.pend_sel = (st >> 16) & 1u;
+    U.full = (st >> 17) & 1u;
+    U.span = st >> 24;
+    U.b = s_pub[kPubB];
+    U.W = s_pub[kPubW];
+    U.epoch = s_pub[kPubEpoch];
+    U.hround = s_pub[kPubHround];
+    U.inst = s_pub[kPubInst];
+    U.items = s_pub[kPubItems];
 }
 
 // Grid barrier after a phase.  The CTA that arrives last decides the next
 // phase (control_step); while the next phase is small it runs it alone and
-// decides again, and only then releases the waiting CTAs, which adopt the
-// published state.  Every wait is bounded by a.wait_ns (globaltimer); on
-// expiry the error word is set and every CTA leaves at its next check.  A
-// solo stretch stops after a.wait_ns / 4 so the waiting CTAs never time out.
+// decides again, and only then releases the waiting CTAs: one fence, then the
+// decision as kPubWords relaxed 64-bit stores tagged with the new generation.
+// Warp 0 of a waiting CTA polls those words (one lane each) until every one
+// carries the new generation, so the poll that sees the release also brings
+// the state.  Every wait is bounded by a.wait_ns (globaltimer); on expiry the
+// error word is set and every CTA leaves at its next check.  A solo stretch
+// stops after a.wait_ns / 4 so the waiting CTAs never time out.
 template <int WT, bool Batch>
 __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U, WarpScratch *scr,
                                                    uint32_t &imp) {
     Ctl *ctl = a.ws.ctl;
+    const unsigned FULL = 0xffffffffu;
     __shared__ uint32_t s_flag[2];
-    __shared__ uint32_t s_pub[10];
+    __shared__ uint32_t s_pub[kPubWords];
     __syncthreads();
     if (threadIdx.x == 0) {
         // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
@@ -826,17 +834,15 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
         s_flag[0] = last;
     }
     __syncthreads();
+    const unsigned long long tag = (unsigned long long)(U.gen + 1u) << 32;
     if (s_flag[0]) {
         const unsigned long long ts = globaltimer();
         bool was_solo = false;
         for (;;) {
             if (threadIdx.x < 32) {
                 bool solo = false;
-                control_step<Batch>(a, U, was_solo, solo);
-                if (threadIdx.x == 0) {
-                    s_flag[1] = solo && (globaltimer() - ts) < a.wait_ns / 4;
-                    fetch_published(ctl, s_pub);
-                }
+                control_step<Batch>(a, U, was_solo, solo, s_pub);
+                if (threadIdx.x == 0) s_flag[1] = solo && (globaltimer() - ts) < a.wait_ns / 4;
             }
             __syncthreads();
             adopt_published(s_pub, U);
@@ -852,26 +858,45 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             __syncthreads();
             was_solo = true;
         }
-        if (threadIdx.x == 0) {
-            ctl->bar_count = 0;
+        // each publishing lane fences before its own store (a release
+        // pattern per word); lane 0's word also releases the counter reset
+        if (threadIdx.x < kPubWords) {
+            if (threadIdx.x == 0) ctl->bar_count = 0;
             __threadfence();
-            st_release(&ctl->bar_gen, U.gen + 1u);
+            st_relaxed64(&ctl->pubw[threadIdx.x], tag | s_pub[threadIdx.x]);
         }
     } else {
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            const unsigned lane = lane_id();
             const unsigned long long t0 = globaltimer();
             uint32_t spins = 0;
-            while (ld_acquire(&ctl->bar_gen) != U.gen + 1u) {
+            unsigned long long v = tag;
+            bool quit = false;
+            for (;;) {
+                if (lane < kPubWords) v = ld_relaxed64(&ctl->pubw[lane]);
+                if (__all_sync(FULL, (v & 0xFFFFFFFF00000000ull) == tag)) break;
                 if ((++spins & 255u) == 0) {
-                    if (ld_relaxed(&ctl->error) != 0) break;
-                    if (globaltimer() - t0 > a.wait_ns) {
-                        atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
+                    int stop = 0;
+                    if (lane == 0) {
+                        if (ld_relaxed(&ctl->error) != 0) {
+                            stop = 1;
+                        } else if (globaltimer() - t0 > a.wait_ns) {
+                            atomicCAS(&ctl->error, 0u, (uint32_t)kErrTimeout);
+                            stop = 1;
+                        }
+                    }
+                    if (__shfl_sync(FULL, stop, 0)) {
+                        quit = true;
                         break;
                     }
                 }
             }
             __threadfence();
-            fetch_published(ctl, s_pub);
+            if (lane < kPubWords) s_pub[lane] = (uint32_t)v;
+            __syncwarp();
+            // after an error or a timeout this CTA stops; an error raised
+            // during the phase reaches the others through the next decision
+            if (lane == 0 && quit) s_pub[kPubState] = (s_pub[kPubState] & ~0xFFu) | (uint32_t)kPhDone;
         }
         __syncthreads();
         adopt_published(s_pub, U);
@@ -896,6 +921,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     U.inst = kNoInst;
     U.span = ld_relaxed(&ctl->pub_span);
     U.full = ld_relaxed(&ctl->pub_full);
+    U.items = kNoItems;
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t imp = 0;
@@ -938,6 +964,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Works
     U.inst = kNoInst;
     U.span = 1;
     U.full = 0;
+    U.items = kNoItems;
     U.gen = 0;
     U.t0 = globaltimer();
     uint32_t loaded = kNoInst;
