@@ -641,9 +641,12 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dis
 
 // One SSSP with the schedule the flags ask for.  GBS_F_LEARNED: the first
 // learned run on a graph is preceded by a plain run that times the plain
-// schedule; a learned run that passes (1 + margin) x that time stops, the
-// plain schedule runs instead, and later learned calls on the graph run the
-// plain schedule directly.  Reported times include every run the call made.
+// schedule; a learned run that passes (1 + margin) x that time stops and the
+// plain schedule runs instead.  When that plain run finished within the limit
+// the controller lost, and later learned calls on the graph run the plain
+// schedule directly; otherwise the source is just longer than the one timed
+// and the plain time is raised to it.  Reported times include every run the
+// call made.
 gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_dev, int32_t *pred_dev,
                     gbs_stats *stats) {
     const bool learned = p && (p->flags & GBS_F_LEARNED);
@@ -678,8 +681,13 @@ gbs_status run_sssp(gbs_graph *g, uint32_t src, const gbs_params *p, void *dist_
     }
     st = launch_run(g, src, &plain, dist_dev, pred_dev, &rs, false, nullptr);
     if (st != GBS_OK) return st;
+    // the learned run was stopped at the limit; it lost if the plain schedule
+    // finished this source within that limit (5% timing noise allowed).  A
+    // source whose plain run itself takes longer says nothing about the
+    // controller: the limit grows to it instead.
+    const double limit_ms = g->plain_ms * (1.0 + g->ctrl_margin);
+    if (rs.kernel_ms <= limit_ms * 1.05) g->ctrl_lost = true;
     g->plain_ms = std::max(g->plain_ms, rs.kernel_ms);
-    g->ctrl_lost = true;
     rs.kernel_ms += ps.kernel_ms + ls.kernel_ms;
     rs.device_ms += ps.device_ms + ls.device_ms;
     rs.learned = 3u;

@@ -343,10 +343,12 @@ gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *c
  * params: 5410 floats: input means[16], input scales[16], W1[16][64], b1[64],
  * W2[64][64], b2[64], W3[64][2], b3[2] (row-major, inputs first).  margin
  * (<= 0: 0.25): a learned run that runs longer than (1 + margin) times the
- * plain schedule on this graph stops and the plain schedule runs instead; from
- * then on GBS_F_LEARNED calls on the graph run the plain schedule (until the
- * controller is set again).  The first learned run on a graph times the plain
- * schedule first.  The
+ * plain schedule on this graph stops and the plain schedule runs instead.  If
+ * that plain run finished within the limit (5% timing noise allowed), the
+ * controller lost: from then on GBS_F_LEARNED calls on the graph run the plain
+ * schedule (until the controller is set again); otherwise the plain time the
+ * limit is based on rises to that run's.  The first learned run on a graph
+ * times the plain schedule first.  The
  * distances and predecessors never depend on the schedule.  params NULL
  * removes the controller.  The trace records of a run carry each bucket's
  * span (bits 8-15 of kind) and whether it relaxed whole rows (bit 16).

@@ -151,6 +151,32 @@ def test_learned_guard_falls_back_to_plain(gb, orc):
 
 
 @pytest.mark.gpu
+def test_learned_guard_longer_source_is_not_a_loss(gb, orc):
+    """The guard's plain time comes from the first source.  A later source
+    whose plain run alone exceeds the limit stops its learned run, but that is
+    not a loss: the limit rises to that plain time and the next learned call
+    runs the controller.  Graph: a 4-vertex path (timed first) beside a 200^2
+    grid."""
+    from graphbench_gb300 import controller
+    grid = gb.gen_grid(200, 200, 5, "f32")
+    gr = grid.row.astype(np.int64)
+    row = np.concatenate([[0, 1, 3, 5], 6 + gr]).astype(np.uint32)
+    col = np.concatenate([[1, 0, 2, 1, 3, 2], grid.col.astype(np.int64) + 4]).astype(np.uint32)
+    w = np.concatenate([np.full(6, 2.0, np.float32), grid.w]).astype(np.float32)
+    src = 4 + 200 * 100 + 100
+    with gb.Graph(row, col, w) as g:
+        g.set_controller(controller.load(), margin=10.0)
+        _, _, st0 = g.sssp(0, flags=gb.F_LEARNED)      # times plain on the path
+        assert st0["learned"] == 1
+        d1, _, st1 = g.sssp(src, flags=gb.F_LEARNED)   # passes 11x the path's time
+        assert st1["learned"] == 3
+        d2, _, st2 = g.sssp(src, flags=gb.F_LEARNED)
+        assert st2["learned"] == 1                     # not lost: the controller runs
+    ref_d = orc.dijkstra(row, col, w, src)
+    assert np.array_equal(d1, ref_d) and np.array_equal(d2, ref_d)
+
+
+@pytest.mark.gpu
 def test_trained_controller_beats_plain_on_held_out_graphs(gb):
     """The committed controller on graphs and seeds outside its training set:
     total kernel time of learned runs below the plain fixed delta's (a call
