@@ -420,7 +420,9 @@ typedef struct gbs_batch_params {
     double light;          /* >= 0: light bound of every instance; < 0: the
                               instance's delta; +INFINITY: no split (every edge
                               light) */
-    uint32_t group_ctas;   /* CTAs per group (0: chosen from the instance count) */
+    uint32_t group_ctas;   /* CTAs per group (0: one group per instance while the
+                              groups' distance words, 8 bytes per vertex each,
+                              fit in L2; fewer and wider groups beyond) */
     uint32_t flags;        /* GBS_F_NO_SOLO */
     uint32_t wait_limit_ms;
     uint32_t solo_entries;
