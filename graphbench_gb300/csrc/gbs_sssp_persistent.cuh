@@ -188,15 +188,18 @@ __device__ __forceinline__ void relax_chunk(const SsspArgs &a, const Targets &t,
 // One thread per heavy descriptor, with dist(u) read from dp: u's distance
 // after the bucket's light loop.  Chunks longer than kInlineEdges are relaxed
 // one after another by the whole warp; the shorter ones (most heavy ranges of
-// a sparse graph) together, packed across the warp by a prefix sum.
+// a sparse graph) together, packed across the warp by a prefix sum.  Lane l
+// of warp w takes descriptors w + nwarps * (32 k + l): the consecutive
+// descriptors of one long row (a hub's heavy range is hundreds of them) go
+// to different warps instead of queueing up in one.
 template <int WT>
 __device__ void relax_heavy(const SsspArgs &a, const Targets &t, const Exec &x, uint32_t count, uint32_t &imp) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     uint32_t nc = 0;   // candidates buffered by this warp
     uint32_t my_edges = 0;
-    for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
-        const uint32_t i = base + lane;
+    for (unsigned long long j0 = 0; x.warp + (unsigned long long)x.nwarps * j0 < count; j0 += 32u) {
+        const unsigned long long i = x.warp + (unsigned long long)x.nwarps * (j0 + lane);
         uint32_t u = 0, s = 0, len = 0;
         typename Arith<WT>::D du = 0;
         if (i < count) {
