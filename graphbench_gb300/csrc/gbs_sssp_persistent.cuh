@@ -58,6 +58,34 @@ __device__ __forceinline__ uint32_t pack_state(const Uniform &N) {
            ((N.span & 0xFFu) << 24);
 }
 
+// Writes a warp's descriptors.  Lane l owns descriptors [excl_l, excl_l + n_l)
+// of the warp's `total` (exclusive prefix excl); its descriptor c covers edges
+// [s_l + c kDescEdges, min(e_l, s_l + (c + 1) kDescEdges)) of row u_l and
+// carries y_l.  The 32 lanes write them together, 32 per round (each finds the
+// owning lane by a binary search over excl), so the hundreds of descriptors
+// of a hub row do not queue on its lane.
+__device__ __forceinline__ void write_descs(uint4 *out, uint32_t base, uint32_t total, uint32_t excl, uint32_t u,
+                                            uint32_t y, uint32_t s, uint32_t e) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    for (uint32_t k0 = 0; k0 < total; k0 += 32u) {
+        const uint32_t k = k0 + lane;
+        uint32_t own = 0;   // the largest lane whose excl <= k
+#pragma unroll
+        for (uint32_t b = 16; b > 0; b >>= 1) {
+            const uint32_t x = __shfl_sync(FULL, excl, own + b);
+            if (x <= k) own += b;
+        }
+        const uint32_t ou = __shfl_sync(FULL, u, own), oy = __shfl_sync(FULL, y, own);
+        const uint32_t os = __shfl_sync(FULL, s, own), oe = __shfl_sync(FULL, e, own);
+        const uint32_t ox = __shfl_sync(FULL, excl, own);
+        if (k < total) {
+            const uint32_t cs = os + (k - ox) * kDescEdges;
+            out[base + k] = make_uint4(ou, oy, cs, min(oe, cs + kDescEdges));
+        }
+    }
+}
+
 // ------------------------------------------------------------------- SCAN
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
@@ -109,15 +137,11 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             uint32_t dbase = 0;
             if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt.v, total);
             dbase = __shfl_sync(FULL, dbase, 31);
-            const uint32_t pos = dbase + incl - nd;
-            if (pos + nd <= a.ws.desc_cap) {
-                for (uint32_t c = 0; c < nd; ++c) {
-                    const uint32_t cs = s + c * kDescEdges;
-                    // float64 distances do not fit the descriptor: the
-                    // relaxation reads dp[u] again (a fresher value is as valid)
-                    a.ws.desc[pos + c] = make_uint4(u, WT == kWF64 ? 0u : (uint32_t)du, cs, min(e, cs + kDescEdges));
-                }
-            } else if (nd) {
+            if (dbase + total <= a.ws.desc_cap) {
+                // float64 distances do not fit the descriptor: the relaxation
+                // reads dp[u] again (a fresher value is as valid)
+                write_descs(a.ws.desc, dbase, total, incl - nd, u, WT == kWF64 ? 0u : (uint32_t)du, s, e);
+            } else if (lane == 31) {
                 atomicExch(&ctl->error, (uint32_t)kErrCapacity);
             }
             my_edges += nd ? len : 0u;
@@ -138,13 +162,9 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
                 uint32_t hbase = 0;
                 if (lane == 31) hbase = atomicAdd(&ctl->hdesc_cnt.v, htotal);
                 hbase = __shfl_sync(FULL, hbase, 31);
-                const uint32_t pos = hbase + hincl - hn;
-                if (pos + hn <= a.ws.desc_cap) {
-                    for (uint32_t c = 0; c < hn; ++c) {
-                        const uint32_t cs = e + c * kDescEdges;
-                        a.ws.hdesc[pos + c] = make_uint4(u, 0u, cs, min(he, cs + kDescEdges));
-                    }
-                } else if (hn) {
+                if (hbase + htotal <= a.ws.desc_cap) {
+                    write_descs(a.ws.hdesc, hbase, htotal, hincl - hn, u, 0u, e, he);
+                } else if (lane == 31) {
                     atomicExch(&ctl->error, (uint32_t)kErrCapacity);
                 }
             }
