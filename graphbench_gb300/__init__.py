@@ -201,11 +201,11 @@ def _load() -> ctypes.CDLL:
     L.gbs_bc.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
     L.gbs_bc_device.argtypes = [P, P, ctypes.c_uint32, ctypes.POINTER(Params), P, ctypes.POINTER(BcStats)]
     L.gbs_read_text.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(P), ctypes.POINTER(IngestInfo)]
-    L.gbs_parse_text.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(P),
+    L.gbs_parse_text.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(P),
                                  ctypes.POINTER(IngestInfo)]
     L.gbs_read_bin.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(P),
                                ctypes.POINTER(IngestInfo)]
-    L.gbs_parse_bin.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+    L.gbs_parse_bin.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
                                 ctypes.POINTER(P), ctypes.POINTER(IngestInfo)]
     L.gbs_device_csr_info.argtypes = [P, P, P]
     L.gbs_device_csr_export.argtypes = [P, P, P, P]
@@ -580,6 +580,16 @@ class Graph:
 DIR_RECV, DIR_SEND = 0, 1
 
 
+def _bytes_arg(data):
+    """(pointer, length) of a bytes object or a contiguous uint8 array."""
+    if isinstance(data, np.ndarray):
+        if data.dtype != np.uint8 or not data.flags["C_CONTIGUOUS"]:
+            raise TypeError("file image arrays must be contiguous uint8")
+        return ctypes.c_void_p(data.ctypes.data), data.nbytes
+    data = bytes(data) if not isinstance(data, bytes) else data
+    return ctypes.cast(ctypes.c_char_p(data), ctypes.c_void_p), len(data)
+
+
 class DeviceCsr:
     """A graph read on the GPU (gbs_read_text / gbs_read_bin and the parse_*
     variants over bytes), laid out as the reference's readers lay out their
@@ -600,9 +610,11 @@ class DeviceCsr:
         return cls(h, info)
 
     @classmethod
-    def parse_text(cls, data: bytes, direction: int = DIR_SEND) -> "DeviceCsr":
+    def parse_text(cls, data, direction: int = DIR_SEND) -> "DeviceCsr":
+        """data: bytes, or a contiguous uint8 array (e.g. a PinnedBuffer's)."""
         h, info = ctypes.c_void_p(), IngestInfo()
-        _check(lib.gbs_parse_text(data, len(data), direction, ctypes.byref(h), ctypes.byref(info)), "gbs_parse_text")
+        ptr, n = _bytes_arg(data)
+        _check(lib.gbs_parse_text(ptr, n, direction, ctypes.byref(h), ctypes.byref(info)), "gbs_parse_text")
         return cls(h, info)
 
     @classmethod
@@ -613,10 +625,12 @@ class DeviceCsr:
         return cls(h, info)
 
     @classmethod
-    def parse_bin(cls, data: bytes, direction: int = DIR_SEND, target_offset: int = 1,
+    def parse_bin(cls, data, direction: int = DIR_SEND, target_offset: int = 1,
                   dedup: bool = False) -> "DeviceCsr":
+        """data: bytes, or a contiguous uint8 array (e.g. a PinnedBuffer's)."""
         h, info = ctypes.c_void_p(), IngestInfo()
-        _check(lib.gbs_parse_bin(data, len(data), direction, target_offset, int(bool(dedup)), ctypes.byref(h),
+        ptr, n = _bytes_arg(data)
+        _check(lib.gbs_parse_bin(ptr, n, direction, target_offset, int(bool(dedup)), ctypes.byref(h),
                                  ctypes.byref(info)), "gbs_parse_bin")
         return cls(h, info)
 

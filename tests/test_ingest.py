@@ -84,13 +84,20 @@ def _need_gpu(gb):
 
 
 def _gpu_read(gb, case, from_bytes=False):
+    """from_bytes: False reads the file, True parses its bytes, "pinned"
+    parses them from a page-locked uint8 array."""
     path = FILES / case["file"]
+    data = path.read_bytes()
+    if from_bytes == "pinned":
+        pin = gb.PinnedBuffer(len(data), np.uint8)
+        pin.array[:] = np.frombuffer(data, dtype=np.uint8)
+        data = pin.array
     if case["kind"] == "text":
         if from_bytes:
-            return gb.DeviceCsr.parse_text(path.read_bytes(), case["direction"])
+            return gb.DeviceCsr.parse_text(data, case["direction"])
         return gb.DeviceCsr.read_text(path, case["direction"])
     if from_bytes:
-        return gb.DeviceCsr.parse_bin(path.read_bytes(), case["direction"], 1, case["dedup"])
+        return gb.DeviceCsr.parse_bin(data, case["direction"], 1, case["dedup"])
     return gb.DeviceCsr.read_bin(path, case["direction"], 1, case["dedup"])
 
 
@@ -98,7 +105,7 @@ def _gpu_read(gb, case, from_bytes=False):
 @pytest.mark.parametrize("case", CASES, ids=_ids)
 def test_gpu_reader_matches_reference_golden(case, gb):
     _need_gpu(gb)
-    for from_bytes in (False, True):
+    for from_bytes in (False, True, "pinned"):
         with _gpu_read(gb, case, from_bytes) as c:
             row, col, w = c.export()
             assert (sha(row), sha(col), sha(w)) == (case["row_sha"], case["col_sha"], case["w_sha"])
