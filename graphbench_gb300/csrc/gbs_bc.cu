@@ -604,12 +604,22 @@ __device__ __forceinline__ void forward_rows(const BcArgs &a, Stage &st, uint32_
     push_flat(a, st, bits, beg, su);
 }
 
-// FORWARD for the words x0 + lane < whi of the level's long rows.
-__device__ __forceinline__ void forward_words(const BcArgs &a, Stage &st, uint32_t x0, uint32_t whi) {
+// Words of the word space one warp takes at a time: 32 consecutive ones on
+// a big level, fewer on a level of few (hub) words so that every warp gets
+// some (a hub word holds up to 32 tight edges, and one warp working through
+// 32 of them while the others wait at the barrier was the cost of such
+// levels).  The mapping changes no result: every word's sum is formed alone.
+__device__ __forceinline__ uint32_t words_per_warp(uint32_t words, uint32_t nwarps) {
+    const uint32_t c = (words + nwarps - 1u) / nwarps;
+    return c < 1u ? 1u : (c > 32u ? 32u : c);
+}
+
+// FORWARD for the words x0 + lane < xe of the level's long rows.
+__device__ __forceinline__ void forward_words(const BcArgs &a, Stage &st, uint32_t x0, uint32_t xe) {
     const uint32_t x = x0 + (threadIdx.x & 31u);
     unsigned long long su = 0;
     uint32_t bits = 0, W = 0;
-    if (x < whi) {
+    if (x < xe) {
         const SpaceWord sw = space_word(a, x);
         bits = sw.bits;
         W = sw.W;
@@ -647,18 +657,18 @@ __device__ __forceinline__ void backward_rows(const BcArgs &a, uint32_t i0, uint
     }
 }
 
-// BACKWARD for the words x0 + lane < whi of the level's long rows: each
+// BACKWARD for the words x0 + lane < xe of the level's long rows: each
 // word's sum goes to vw_part.
-__device__ __forceinline__ void backward_words(const BcArgs &a, uint32_t x0, uint32_t whi) {
+__device__ __forceinline__ void backward_words(const BcArgs &a, uint32_t x0, uint32_t xe) {
     const uint32_t x = x0 + (threadIdx.x & 31u);
     SpaceWord sw{};
     unsigned long long su = 0;
-    if (x < whi) {
+    if (x < xe) {
         sw = space_word(a, x);
         if (sw.bits) su = __ldcg(a.sigma + sw.u);
     }
     const double p = word_sums(a, sw.W, sw.bits, su);
-    if (x < whi) a.vw_part[x] = p;
+    if (x < xe) a.vw_part[x] = p;
 }
 
 // BACKWARD, after backward_words: delta of long rows.  Each block of 32 word
@@ -760,7 +770,8 @@ __global__ void __launch_bounds__(kTPB, 1) bc_dag(BcArgs a) {
         const uint32_t lo = s_pub[0], hi = s_pub[1], wlo = s_pub[2], whi = s_pub[3], shi = s_pub[5];
         if (lo >= hi) break;
         for (uint32_t i0 = lo + gwarp * 32u; i0 < hi; i0 += nwarps * 32u) forward_rows(a, st, i0, hi);
-        for (uint32_t x0 = wlo + gwarp * 32u; x0 < whi; x0 += nwarps * 32u) forward_words(a, st, x0, whi);
+        const uint32_t cw = words_per_warp(whi - wlo, nwarps);
+        for (uint32_t x0 = wlo + gwarp * cw; x0 < whi; x0 += nwarps * cw) forward_words(a, st, x0, min(x0 + cw, whi));
         flush_appends(a, st);
         auto next = [&]() {
             trace_phase(a, kTrForward, L, hi - lo, whi - wlo);
@@ -789,7 +800,8 @@ __global__ void __launch_bounds__(kTPB, 1) bc_dag(BcArgs a) {
         const uint32_t lo = __ldcg(a.lvl + k), hi = __ldcg(a.lvl + k + 1);
         const uint32_t wlo = __ldcg(a.wlv + k), whi = __ldcg(a.wlv + k + 1);
         for (uint32_t i0 = lo + gwarp * 32u; i0 < hi; i0 += nwarps * 32u) backward_rows(a, i0, hi);
-        for (uint32_t x0 = wlo + gwarp * 32u; x0 < whi; x0 += nwarps * 32u) backward_words(a, x0, whi);
+        const uint32_t cw = words_per_warp(whi - wlo, nwarps);
+        for (uint32_t x0 = wlo + gwarp * cw; x0 < whi; x0 += nwarps * cw) backward_words(a, x0, min(x0 + cw, whi));
         if (whi > wlo) {   // the level's long rows: add up their word sums
             auto words_done = [&]() { trace_phase(a, kTrBackwardWords, k, hi - lo, whi - wlo); };
             if (!grid_step(a, gen, s_pub, words_done)) return;
