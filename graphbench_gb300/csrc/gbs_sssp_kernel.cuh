@@ -123,11 +123,12 @@ __device__ __forceinline__ uint32_t bucket_of(typename Arith<WT>::D d, const Sss
 }
 
 constexpr int kQueues = kNB + 2;   // next frontier, kNB ring lists, pending
-constexpr int kCand = 64;          // candidate buffer: < 32 kept + <= 32 per append
+constexpr int kFlush = 64;         // candidates per atomic round (two per lane)
+constexpr int kCand = kFlush + 32; // candidate buffer: < kFlush kept + <= 32 per append
 
 // Per-warp shared-memory scratch.
 struct WarpScratch {
-    uint32_t bins[2 * kQueues];    // enqueue histogram and list bases
+    uint32_t cnt[kQueues];         // enqueue histogram
     uint32_t cv[kCand];            // candidate target
     uint32_t cnd[kCand];           // candidate tentative distance bits (low word)
     uint32_t cu[kCand];            // candidate source; float64 runs: distance high word
@@ -161,7 +162,9 @@ __device__ __forceinline__ uint32_t *queue_list(const SsspArgs &a, const Targets
 // Appends every (q[j], v[j]) with q[j] >= 0 of the whole warp.  A
 // shared-memory histogram over the kQueues target lists gives each item its
 // rank; then lanes reserve space for all non-empty lists at once (one global
-// atomic per list, all in flight together) and every item is written.
+// atomic per list, all in flight together; lane l reserves lists l, l + 32
+// and l + 64) and every item is written at the base its list's lane hands
+// over by shuffle.
 template <int U>
 __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t, const int (&q)[U],
                                              const uint32_t (&v)[U]) {
@@ -171,7 +174,7 @@ __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t
 #pragma unroll
     for (int j = 0; j < U; ++j) has |= (q[j] >= 0 ? 1u : 0u) << j;
     if (__ballot_sync(FULL, has != 0) == 0) return;
-    uint32_t *cnt = t.scr->bins, *base = t.scr->bins + kQueues;
+    uint32_t *cnt = t.scr->cnt;
     for (int i = (int)lane; i < kQueues; i += 32) cnt[i] = 0;
     __syncwarp();
     uint32_t rank[U];
@@ -183,15 +186,15 @@ __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t
     const uint32_t b0 = c0 ? atomicAdd(queue_counter(a, t, i0), c0) : 0u;
     const uint32_t b1 = c1 ? atomicAdd(queue_counter(a, t, i1), c1) : 0u;
     const uint32_t b2 = c2 ? atomicAdd(queue_counter(a, t, i2), c2) : 0u;
-    if (c0) base[i0] = b0;
-    if (c1) base[i1] = b1;
-    if (c2) base[i2] = b2;
-    __syncwarp();
     const uint32_t n = a.g.n;
 #pragma unroll
     for (int j = 0; j < U; ++j) {
-        if ((has >> j) & 1u) {
-            const uint32_t pos = base[q[j]] + rank[j];
+        const bool mine = (has >> j) & 1u;
+        const int src = mine ? (q[j] & 31) : 0;
+        const uint32_t x0 = __shfl_sync(FULL, b0, src), x1 = __shfl_sync(FULL, b1, src);
+        const uint32_t x2 = __shfl_sync(FULL, b2, src);
+        if (mine) {
+            const uint32_t pos = (q[j] < 32 ? x0 : q[j] < 64 ? x1 : x2) + rank[j];
             if (pos < n) queue_list(a, t, q[j])[pos] = v[j];
             else atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
         }
@@ -282,39 +285,44 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
     }
 }
 
-// Warp-collective tail of one relaxation round: U edges per lane whose
-// targets and weights are loaded (val[j] = the lane has an edge in slot j).
-// Runs the atomic part (improve_batch + enqueue) on the top `take` (<= 32)
-// candidates of the warp's buffer, one per lane.
-template <int WT>
+// Runs the atomic part (improve_batch + enqueue) on the top `take`
+// (<= 32 U) candidates of the warp's buffer, U per lane: one chain of
+// dependent atomics (distance, tag, list) per U x 32 candidates.
+template <int WT, int U>
 __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t take,
                                            uint32_t &imp) {
     const unsigned lane = lane_id();
     WarpScratch *s = t.scr;
-    const bool has = lane < take;
-    const uint32_t i = nc - take + lane;
-    uint32_t v1[1] = {has ? s->cv[i] : 0u};
-    uint32_t u1[1] = {has ? s->cu[i] : 0u};
-    typename Arith<WT>::D n1[1];
-    if constexpr (WT == kWF64) {
-        n1[0] = has ? (((unsigned long long)s->cu[i] << 32) | s->cnd[i]) : 0ull;
-        u1[0] = 0u;
-    } else {
-        n1[0] = has ? s->cnd[i] : 0u;
+    uint32_t v1[U], u1[U];
+    typename Arith<WT>::D n1[U];
+    bool c1[U];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+        const uint32_t k = lane + 32u * (uint32_t)j;
+        const bool has = k < take;
+        const uint32_t i = nc - take + k;
+        c1[j] = has;
+        v1[j] = has ? s->cv[i] : 0u;
+        u1[j] = has ? s->cu[i] : 0u;
+        if constexpr (WT == kWF64) {
+            n1[j] = has ? (((unsigned long long)s->cu[i] << 32) | s->cnd[i]) : 0ull;
+            u1[j] = 0u;
+        } else {
+            n1[j] = has ? s->cnd[i] : 0u;
+        }
     }
-    const bool c1[1] = {has};
     __syncwarp();
     nc -= take;
-    int q[1];
-    improve_batch<WT, 1>(a, t, c1, v1, u1, n1, q, imp);
-    warp_enqueue<1>(a, t, q, v1);
+    int q[U];
+    improve_batch<WT, U>(a, t, c1, v1, u1, n1, q, imp);
+    warp_enqueue<U>(a, t, q, v1);
 }
 
 // Warp-collective tail of one relaxation round: U edges per lane whose
 // targets and weights are loaded (val[j] = the lane has an edge in slot j).
 // Only edges that pass the read-only filter (packed tentative value below
 // the current dp) become candidates; they collect in the warp's shared-memory
-// buffer and the atomic chain runs once per 32 of them, not once per round.
+// buffer and the atomic chain runs once per kFlush of them, not once per round.
 template <int WT, int U>
 __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Targets &t, const bool (&val)[U],
                                                  const uint32_t (&v)[U], const typename Arith<WT>::Wt (&w)[U],
@@ -345,7 +353,7 @@ __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Target
             }
             nc += (uint32_t)__popc(m);
             __syncwarp();
-            if (nc >= 32u) cand_flush<WT>(a, t, nc, 32u, imp);
+            if (nc >= (uint32_t)kFlush) cand_flush<WT, kFlush / 32>(a, t, nc, kFlush, imp);
         }
     }
 }
@@ -353,7 +361,8 @@ __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Target
 // Drains the warp's candidate buffer (end of a phase's relaxation work).
 template <int WT>
 __device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t &imp) {
-    if (nc) cand_flush<WT>(a, t, nc, nc, imp);
+    if (nc > 32u) cand_flush<WT, kFlush / 32>(a, t, nc, nc, imp);
+    else if (nc) cand_flush<WT, 1>(a, t, nc, nc, imp);
 }
 
 // Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
