@@ -873,11 +873,11 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             __syncthreads();
             if (!solo) break;
             run_phase<WT>(a, U, cta_exec(), scr, imp);
-            // atomics whose result is unused (tag and pend_min minima) are
-            // fire-and-forget reductions; each thread waits until its own have
-            // reached L2 before the decision reads the counters and tags they
-            // feed (the grid path gets this from the fence before arrival)
-            __threadfence();
+            // the decision is taken by this CTA: __syncthreads makes every
+            // global access of the phase (the fire-and-forget tag and pend_min
+            // reductions included) visible to all its threads, as it does for
+            // the other CTAs' arrivals, where thread 0 alone fences before the
+            // arrival; the release after the stretch fences before publishing
             __syncthreads();
             was_solo = true;
         }
