@@ -242,6 +242,18 @@ __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long l
 __device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned long long v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// Barrier arrival: release (this CTA's phase, made visible to thread 0 by
+// __syncthreads) and acquire (every earlier arrival's phase) in one atomic.
+__device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

@@ -849,11 +849,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
         // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
         const bool stall = (a.flags & GBS_F_TEST_STALL) && U.gen == 0 && group_rank(a) == 0;
         uint32_t last = 0;
-        if (!stall) {
-            __threadfence();
-            last = atomicAdd(&ctl->bar_count, 1u) == a.group_ctas - 1u;
-            if (last) __threadfence();
-        }
+        if (!stall) last = atom_add_acq_rel(&ctl->bar_count, 1u) == a.group_ctas - 1u;
         s_flag[0] = last;
     }
     __syncthreads();
@@ -896,7 +892,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             unsigned long long v = tag;
             bool quit = false;
             for (;;) {
-                if (lane < kPubWords) v = ld_relaxed64(&ctl->pubw[lane]);
+                if (lane < kPubWords) v = ld_acquire64(&ctl->pubw[lane]);
                 if (__all_sync(FULL, (v & 0xFFFFFFFF00000000ull) == tag)) break;
                 if ((++spins & 255u) == 0) {
                     int stop = 0;
@@ -914,7 +910,6 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
                     }
                 }
             }
-            __threadfence();
             if (lane < kPubWords) s_pub[lane] = (uint32_t)v;
             __syncwarp();
             // after an error or a timeout this CTA stops; an error raised
