@@ -202,14 +202,11 @@ __device__ __forceinline__ bool grid_step(const BcArgs &a, uint32_t &gen, uint32
     __syncthreads();
     if (threadIdx.x == 0) {
         BcCtl *c = a.ctl;
-        __threadfence();
-        const bool last = atomicAdd(&c->bar_count, 1u) == a.nblocks - 1u;
+        const bool last = atom_add_acq_rel(&c->bar_count, 1u) == a.nblocks - 1u;
         if (last) {
-            __threadfence();
             decide();
             c->bar_count = 0;
-            __threadfence();
-            st_release(&c->bar_gen, gen + 1u);
+            st_release(&c->bar_gen, gen + 1u);   // releases the decision and the reset
         } else {
             const unsigned long long t0 = globaltimer();
             uint32_t spins = 0;

@@ -239,9 +239,6 @@ __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long l
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
 // Barrier arrival: release (this CTA's phase, made visible to thread 0 by
 // __syncthreads) and acquire (every earlier arrival's phase) in one atomic.
 __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
@@ -253,6 +250,9 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
     unsigned long long v;
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ void st_release64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
     unsigned long long t;

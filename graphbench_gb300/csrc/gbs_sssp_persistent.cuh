@@ -830,8 +830,8 @@ __device__ __forceinline__ void adopt_published(const uint32_t *s_pub, Uniform &
 
 // Grid barrier after a phase.  The CTA that arrives last decides the next
 // phase (control_step); while the next phase is small it runs it alone and
-// decides again, and only then releases the waiting CTAs: one fence, then the
-// decision as kPubWords relaxed 64-bit stores tagged with the new generation.
+// decides again, and only then releases the waiting CTAs: the decision as
+// kPubWords 64-bit release stores tagged with the new generation.
 // Warp 0 of a waiting CTA polls those words (one lane each) until every one
 // carries the new generation, so the poll that sees the release also brings
 // the state.  Every wait is bounded by a.wait_ns (globaltimer); on expiry the
@@ -877,12 +877,10 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             __syncthreads();
             was_solo = true;
         }
-        // each publishing lane fences before its own store (a release
-        // pattern per word); lane 0's word also releases the counter reset
+        // one release store per word; lane 0's also releases the counter reset
         if (threadIdx.x < kPubWords) {
             if (threadIdx.x == 0) ctl->bar_count = 0;
-            __threadfence();
-            st_relaxed64(&ctl->pubw[threadIdx.x], tag | s_pub[threadIdx.x]);
+            st_release64(&ctl->pubw[threadIdx.x], tag | s_pub[threadIdx.x]);
         }
     } else {
         if (threadIdx.x < 32) {
