@@ -80,7 +80,8 @@ typedef struct gbs_params {
                                 descriptors relaxed one warp each; 0 = 32 */
     uint32_t full_items;     /* a bucket whose lists hold at most this many entries
                                 when it starts relaxes whole rows (light and heavy
-                                edges together, no heavy phase); 0 = 1024 */
+                                edges together, no heavy phase); 0 = max(1024,
+                                vertices / 16) */
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
