@@ -1,7 +1,7 @@
 """The learned bucket-width controller.
 
 CPU: the oracle's analytic gradient agrees with finite differences (so it can
-judge the CUDA kernels), and the committed parameter block is well formed.
+check the CUDA kernels), and the committed parameter block is well formed.
 GPU: the CUDA forward/backward kernels' loss and gradient equal the oracle's
 within FP32 tolerance; an Adam step equals the oracle's; training lowers the
 loss; learned runs are bit-identical to plain ones, the guard falls back to
