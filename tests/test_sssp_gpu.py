@@ -119,6 +119,22 @@ def test_solo_phases_same_result(mode, gb, orc):
         assert st2["solo_phases"] > 0
 
 
+@pytest.mark.parametrize("full_items", [1, 0, 1 << 30])
+def test_whole_row_threshold_same_result(full_items, gb, orc):
+    """Buckets of up to full_items entries relax whole rows (0: the default,
+    max(1024, n / 16)); 1 splits every bucket but the source's, 2^30 relaxes
+    every bucket whole.  Distances and predecessors stay the oracle's, and on
+    R-MAT the heavy phases disappear when every bucket is whole."""
+    a = gb.gen_rmat(14, 16, 21)
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, full_items=full_items)
+    _, _, st1 = run_and_check(gb, orc, a.row, a.col, a.w, src, full_items=1)
+    if full_items == 1 << 30:
+        assert st["phases"] < st1["phases"]
+    g2 = gb.gen_grid(48, 80, 7, "f32")
+    run_and_check(gb, orc, g2.row, g2.col, g2.w, 0, full_items=full_items)
+
+
 def test_phase_trace(gb, orc):
     """GBS_F_TRACE records one entry per grid phase; scans are followed by a
     relaxation of the edges they emitted, and device time is monotone."""
