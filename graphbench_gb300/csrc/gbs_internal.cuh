@@ -234,11 +234,6 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
 // Barrier arrival: release (this CTA's phase, made visible to thread 0 by
 // __syncthreads) and acquire (every earlier arrival's phase) in one atomic.
 __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v) {
