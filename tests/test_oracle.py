@@ -123,3 +123,54 @@ def test_reference_list_path_tight_sets(ref_serial):
     roff = np.concatenate([[0], np.cumsum(cnt)])
     for v in range(len(dj)):
         assert sorted(set(lst[roff[v]:roff[v + 1]].tolist())) == sorted(set(preds[off[v]:off[v + 1]].tolist()))
+
+
+def _edge_case_graph():
+    """Multi-edges, self-loops, an isolated vertex and a vertex that only
+    points into the graph (unreachable from 0):
+    0->1 (5), 0->1 (3), 0->0 (2), 1->2 (1), 1->1 (4), 2->0 (7), 2->5 (255),
+    4->3 (9), 5->2 (1)."""
+    edges = {0: [(1, 5), (1, 3), (0, 2)], 1: [(2, 1), (1, 4)], 2: [(0, 7), (5, 255)], 3: [], 4: [(3, 9)],
+             5: [(2, 1)]}
+    row = [0]
+    col, w = [], []
+    for v in range(6):
+        for t, x in edges[v]:
+            col.append(t)
+            w.append(x)
+        row.append(len(col))
+    return (np.array(row, dtype=np.uint64), np.array(col, dtype=np.uint32), np.array(w, dtype=np.uint32))
+
+
+@pytest.mark.parametrize("src", [0, 3, 4])
+@pytest.mark.parametrize("delta", [1, 2, 7, 1000])
+def test_reference_edge_cases(src, delta, ref_serial):
+    """The reference's run_sspath_arr, the oracle's restatement of it and
+    Dijkstra agree on multi-edges (the lighter one counts), self-loops
+    (ignored), a source without out-edges and unreachable vertices (+inf),
+    for deltas below, at and far above the weights."""
+    row, col, w = _edge_case_graph()
+    rd, _ = ref_serial.ref_sssp_arr(row, col, w, src, float(delta))
+    dj = ref_serial.dijkstra(row, col, w, src).astype(np.float64)
+    dj[dj == U32MAX] = np.inf
+    ds, _ = ref_serial.delta_stepping(row, col, w, src, float(delta))
+    assert np.array_equal(rd, dj) and np.array_equal(ds, dj)
+    if src == 0:
+        assert dj.tolist() == [0.0, 3.0, 4.0, np.inf, np.inf, 259.0]
+    if src == 3:
+        assert dj[3] == 0.0 and np.all(np.isinf(np.delete(dj, 3)))
+
+
+@pytest.mark.parametrize("delta", [0.05, 0.4, 2.5])
+def test_reference_matches_oracle_float64_weights(delta, ref_serial):
+    """Fractional double weights (the reference's own readers produce such
+    weights): its run_sspath_arr equals the oracle's float64 Dijkstra bit for
+    bit, because both take the least fixpoint of fl(d[u] + w)."""
+    from oracle import gen
+    row, col, _ = gen.rmat(9, 8, 13)
+    rng = np.random.default_rng(5)
+    w = rng.uniform(0.01, 1.0, len(col))
+    src = gen.max_degree_vertex(row)
+    rd, _ = ref_serial.ref_sssp_arr(row, col, w, src, delta)
+    dj = ref_serial.dijkstra(row, col, w, src)
+    assert np.array_equal(rd, dj)
