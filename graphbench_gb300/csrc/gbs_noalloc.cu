@@ -25,8 +25,17 @@
 // array's device address (cudaGetSymbolAddress; the host-side symbol is only
 // a stand-in) and the persistent kernel's occupancy, and caches both.  Make
 // that first call before any stream capture.
+//
+// Every call waits for its stream before returning: it reads the input check
+// and the run's error word back into host memory.
+//
+// Alignment: adj_dev is read as 8-byte {target, weight} pairs, so it must be
+// 8-byte aligned; row_dev, dist_dev and pred_dev 4-byte aligned.  A pointer
+// that is not is refused on the host before any device work (a misaligned
+// load would be a device fault that ends the context).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -166,6 +175,10 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
         return na_fail(GBS_ERR_INVALID_ARG,
                        "gbs_sssp_noalloc: needs 1 <= n <= 65536 and m <= 2097152 (its scratch is static)");
     if (source >= n) return na_fail(GBS_ERR_INVALID_ARG, "gbs_sssp_noalloc: source out of range");
+    if ((reinterpret_cast<uintptr_t>(adj_dev) & 7u) || (reinterpret_cast<uintptr_t>(row_dev) & 3u) ||
+        (reinterpret_cast<uintptr_t>(dist_dev) & 3u) || (reinterpret_cast<uintptr_t>(pred_dev) & 3u))
+        return na_fail(GBS_ERR_INVALID_ARG,
+                       "gbs_sssp_noalloc: adj_dev must be 8-byte aligned, row_dev / dist_dev / pred_dev 4-byte");
     int dev = 0;
     NA_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return na_fail(GBS_ERR_UNSUPPORTED, "gbs_sssp_noalloc: device index");

@@ -84,7 +84,10 @@ static int set_status(gbs_status st, const char *fn, const char *why) {
 /* The weight type to run in: uint32 when every weight is an integer (exact,
  * the same sums as the reference's doubles), float32 when allowed and every
  * weight is float32-exact, float64 otherwise (the reference's arithmetic);
- * -1 for a negative or non-finite weight. */
+ * -1 for a negative or non-finite weight.  Integer weights whose path sums
+ * reach 2^32 - 1 make the uint32 run report GBS_ERR_OVERFLOW; run_common
+ * then converts the graph again in float64 (exact for integer sums below
+ * 2^53, like the reference's doubles) and runs it there. */
 static int weight_type_of(const t_csr *gs) {
     int all_int = 1, all_f32 = 1;
     for (lint e = 0; e < gs->e_size; ++e) {
@@ -98,18 +101,20 @@ static int weight_type_of(const t_csr *gs) {
     return GBS_WEIGHT_F64;
 }
 
-static gbs_status convert(const t_csr *gs, gbs_graph **out, gbs_weight_type *wt_out, const char **why) {
+static gbs_status convert(const t_csr *gs, int force_f64, gbs_graph **out, gbs_weight_type *wt_out,
+                          const char **why) {
     const lint n = gs->v_size, m = gs->e_size;
     *why = "";
     if (n <= 0 || n >= 0x7FFFFFFFll) { *why = "v_size must be in [1, 2^31)"; return GBS_ERR_INVALID_ARG; }
     if (m < 0 || m >= 0xFFFFFFFFll) { *why = "e_size must be in [0, 2^32)"; return GBS_ERR_UNSUPPORTED; }
     if (!gs->vet_idx || (m && (!gs->edge_idx || !gs->edge_info))) { *why = "NULL CSR array"; return GBS_ERR_INVALID_ARG; }
     if (gs->vet_idx[n - 1] != m) { *why = "vet_idx[v_size-1] != e_size"; return GBS_ERR_INVALID_ARG; }
-    const int wt = weight_type_of(gs);
+    int wt = weight_type_of(gs);
     if (wt < 0) {
         *why = "edge weights must be finite and >= 0";
         return GBS_ERR_INVALID_ARG;
     }
+    if (force_f64) wt = GBS_WEIGHT_F64;
     const size_t wsize = wt == GBS_WEIGHT_F64 ? 8 : 4;
     uint64_t *row = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(n + 1));
     uint32_t *col = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(m ? m : 1));
@@ -159,8 +164,9 @@ done:
     return st;
 }
 
-/* Cached device graph of gs (called with g_mu held). */
-static gbs_status lookup(const t_csr *gs, slot_t **hit, const char **why) {
+/* Cached device graph of gs (called with g_mu held).  force_f64 replaces a
+ * cached uint32 copy by a float64 one (after a uint32 overflow). */
+static gbs_status lookup(const t_csr *gs, int force_f64, slot_t **hit, const char **why) {
     const uint64_t h = sample_hash(gs);
     slot_t *lru = &g_cache[0];
     for (int i = 0; i < CACHE_SLOTS; ++i) {
@@ -168,6 +174,12 @@ static gbs_status lookup(const t_csr *gs, slot_t **hit, const char **why) {
         if (s->g && s->gs == gs && s->vet_idx == gs->vet_idx && s->edge_idx == gs->edge_idx &&
             s->edge_info == gs->edge_info && s->v_size == gs->v_size && s->e_size == gs->e_size &&
             s->sample == h) {
+            if (force_f64 && s->wt != GBS_WEIGHT_F64) {
+                gbs_graph_destroy(s->g);
+                memset(s, 0, sizeof *s);
+                lru = s;
+                break;
+            }
             s->used = ++g_clock;
             *hit = s;
             return GBS_OK;
@@ -181,7 +193,7 @@ static gbs_status lookup(const t_csr *gs, slot_t **hit, const char **why) {
     }
     gbs_weight_type wt = GBS_WEIGHT_U32;
     gbs_graph *g = NULL;
-    const gbs_status st = convert(gs, &g, &wt, why);
+    const gbs_status st = convert(gs, force_f64, &g, &wt, why);
     if (st != GBS_OK) return st;
     lru->gs = gs;
     lru->vet_idx = gs->vet_idx;
@@ -239,7 +251,7 @@ static void run_common(const char *fn, t_csr *gs, p_list *predecesor, lint sourc
         why = "source out of range";
         goto out;
     }
-    st = lookup(gs, &s, &why);
+    st = lookup(gs, 0, &s, &why);
     if (st != GBS_OK) goto out;
     const lint n = gs->v_size;
     dist = malloc(8 * (size_t)n);
@@ -254,6 +266,13 @@ static void run_common(const char *fn, t_csr *gs, p_list *predecesor, lint sourc
     p.delta = delta > 0 ? delta : 0.0;   /* the bucket width, and the light bound (w <= delta) */
     p.light = -1.0;
     st = gbs_sssp(s->g, (uint32_t)source, &p, dist, pred, NULL);
+    if (st == GBS_ERR_OVERFLOW && s->wt == GBS_WEIGHT_U32) {
+        /* integer weights whose path sums do not fit uint32: the same graph
+         * in float64, cached in place of the uint32 copy */
+        st = lookup(gs, 1, &s, &why);
+        if (st != GBS_OK) goto out;
+        st = gbs_sssp(s->g, (uint32_t)source, &p, dist, pred, NULL);
+    }
     if (st != GBS_OK) {
         why = gbs_last_error();
         goto out;

@@ -537,15 +537,19 @@ gbs_status gbs_autotune_plan_pack(gbs_pack *p, const uint32_t *sources, double b
  * device or fail with out-of-memory mid-request) is not acceptable.  The
  * caller passes device buffers it owns:
  *   row_dev  n+1 uint32 exclusive row offsets (row_dev[0] = 0, row_dev[n] = m)
- *   adj_dev  2*m uint32: per edge {target, weight bits}, rows in any order
+ *   adj_dev  2*m uint32: per edge {target, weight bits}, rows in any order;
+ *            read 8 bytes at a time, so adj_dev must be 8-byte aligned
  *   dist_dev n uint32/float32 distances (required), pred_dev n int32 (may be NULL)
+ * row_dev, dist_dev and pred_dev must be 4-byte aligned; a misaligned pointer
+ * returns GBS_ERR_INVALID_ARG before any device work.
  * Weights are uint32 or float32 (>= 0) per wtype; delta <= 0 selects max
  * weight / average out-degree.  Results equal gbs_sssp's bit for bit.
  * Everything else lives in one static device array of about 21 MB that the
  * library holds on every GPU that loads it: n must be at most 65,536 and m at
  * most 2,097,152 (larger inputs return GBS_ERR_INVALID_ARG).  The input CSR is
  * validated on the device first (GBS_ERR_INVALID_ARG if malformed).  Runs on
- * `stream` (a cudaStream_t, NULL = default stream) and returns when done.
+ * `stream` (a cudaStream_t, NULL = default stream) and waits for that stream
+ * before returning (it reads the input check and the error word back).
  * The first call on a device (with that device current) looks up the static
  * array's address and caches it; make that first call before any stream
  * capture.  All calls share the array: calls that overlap on the GPU race and

@@ -20,7 +20,10 @@
  *     address, its array addresses and sizes, and a sample of its contents);
  *     after changing a t_csr in place call gbs_compat_forget(gs);
  *   - edge weights must be finite and >= 0.  Integer weights in [0, 2^32-2]
- *     run in uint32 (exact, equal to the reference's double sums); any other
+ *     run in uint32 (exact, equal to the reference's double sums); when a
+ *     path sum would reach 2^32-1 the call converts the graph again and
+ *     reruns it in float64 (integer sums below 2^53 stay exact), and the
+ *     float64 copy stays cached for later calls on that graph; any other
  *     weights run in float64, the reference's own arithmetic (one rounding
  *     per relaxation), so the distances equal its doubles bit for bit.
  *     gbs_compat_allow_float32(1) runs float32-exact weights in float32

@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY.  Two stages:
 
-1. ``stage()`` (needs the read-only GRAPHBENCH tree, default
-   ``/root/reference``): copies the few source files the SSSP path needs into
+1. ``stage(tree)`` (needs the read-only GRAPHBENCH tree: the argument, or
+   the ``GBREF_TREE`` environment variable): copies the few source files the
+   SSSP path needs into
    ``oracle/_ref/src/`` and applies the minimal patches listed in ``PATCHES``
    there.  Nothing is written outside ``oracle/_ref/``; the tree itself is
    never modified.
@@ -45,7 +46,10 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 SRC_OUT = OUT / "src"
 STUBS = HERE / "stubs"
-DEFAULT_REF = Path(os.environ.get("GBREF_TREE", "/root/reference"))
+def _default_tree() -> Path | None:
+    """The reference tree named by GBREF_TREE, if any."""
+    t = os.environ.get("GBREF_TREE")
+    return Path(t) if t else None
 
 SOURCES = [
     "graph/csr.c",
@@ -108,10 +112,12 @@ def _apply(lines: list[str], anchor: list[str], repl: list[str], name: str) -> l
     return lines[:i] + repl + lines[i + len(anchor):]
 
 
-def stage(ref_tree: Path = DEFAULT_REF) -> bool:
+def stage(ref_tree: Path | None = None) -> bool:
     """Copy + patch the reference sources into oracle/_ref/src.  Returns False
-    when the reference tree is absent (e.g. on a machine that only compiles)."""
-    if not (ref_tree / "sssp" / "csr_sspath_array.c").exists():
+    when no reference tree is given (argument or GBREF_TREE) or it is absent
+    (e.g. on a machine that only compiles the staged sources)."""
+    ref_tree = Path(ref_tree) if ref_tree is not None else _default_tree()
+    if ref_tree is None or not (ref_tree / "sssp" / "csr_sspath_array.c").exists():
         return False
     (SRC_OUT / "include").mkdir(parents=True, exist_ok=True)
     for h in HEADERS:
@@ -159,10 +165,10 @@ def compile_ref(jobs: int = 8) -> list[Path]:
     return outs
 
 
-def build(ref_tree: Path = DEFAULT_REF) -> list[Path]:
+def build(ref_tree: Path | None = None) -> list[Path]:
     stage(ref_tree)
     return compile_ref()
 
 
 if __name__ == "__main__":
-    print(build(Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REF))
+    print(build(Path(sys.argv[1]) if len(sys.argv) > 1 else None))

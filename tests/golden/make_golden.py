@@ -1,8 +1,9 @@
 """Generates the committed golden fixtures in tests/golden/.
 
-Run from the repository root where the reference tree is present:
+Run from the repository root where the reference tree is present, naming
+it in GBREF_TREE:
 
-    python tests/golden/make_golden.py
+    GBREF_TREE=<path of the GRAPHBENCH tree> python tests/golden/make_golden.py
 
 1. ``known_answer.json``: small hand-built graphs with hand-computed distances
    and predecessors.  Before writing, every case is checked against the

@@ -193,6 +193,35 @@ def test_fractional_weights_match_the_reference_doubles(mode, driver, tmp_path, 
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["arr", "list"])
+def test_large_integer_weights_whose_sums_pass_uint32(mode, driver, tmp_path, gb, orc, ref_serial):
+    """Integer weights of 3e9 on a multi-hop path: the sums pass 2^32 - 1, so
+    the uint32 run overflows and the call reruns in float64.  The distances
+    must equal the reference's doubles (integer sums below 2^53 are exact)."""
+    # path 0 -> 1 -> ... -> 7 of weight 3e9 each, plus a cheap shortcut
+    # 0 -> 5 of weight 1 and a back edge 7 -> 0
+    edges = [(i, i + 1, 3.0e9) for i in range(7)] + [(0, 5, 1.0), (7, 0, 2.0)]
+    n = 8
+    edges.sort()
+    row = np.zeros(n + 1, dtype=np.int64)
+    for u, _, _ in edges:
+        row[u + 1] += 1
+    row = np.cumsum(row)
+    col = np.array([v for _, v, _ in edges], dtype=np.int64)
+    w = np.array([x for _, _, x in edges], dtype=np.float64)
+    r, out = run_driver(driver, tmp_path, row, col, w, 0, 1.0e9, mode=mode, reps=2)
+    assert r.returncode == 0 and "status 0" in r.stdout, r.stderr
+    dist, lists = read_output(out, n)
+    want = np.array([0, 3e9, 6e9, 9e9, 12e9, 1.0, 1.0 + 3e9, 1.0 + 6e9])
+    assert np.array_equal(dist, want)
+    refd, _ = ref_serial.ref_sssp_arr(row, col, w, 0, 1.0e9)
+    assert np.array_equal(dist, refd)
+    assert np.array_equal(dist, orc.dijkstra(row.astype(np.uint64), col.astype(np.uint32), w, 0))
+    for v in range(1, n):
+        assert lists[v] == [v - 1 if v != 5 else 0], (v, lists[v])
+
+
+@pytest.mark.gpu
 def test_run_sspath_arr_float32_grid(driver, tmp_path, gb, orc):
     a = gb.gen_grid(40, 50, 3, "f32")
     r, out = run_driver(driver, tmp_path, a.row, a.col, a.w.astype(np.float64), 0, 250.0, extra=("f32",))
