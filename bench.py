@@ -31,6 +31,19 @@ Each reports GTEPS and its ratio to the plain value.
   ingest     the same edges as a shuffled binary edge list parsed on the GPU
              with duplicate removal, CSR and resident graph built there
 
+The other published configurations, each its own record with a parity field
+(oracle Dijkstra and smallest-tight-predecessor rule, run in host threads
+while the GPU works, compared bit for bit; learned / autotuned / batched
+results compared with the plain ones):
+  grid4096_f32   4096 x 4096 grid, float32 weights in [1, 1000), source 0:
+                 plain, autotuned, learned, and 8 sources batched
+  rmat24_u32     R-MAT scale 24, 8 sources: plain, learned, autotuned, batched
+  rmat20_512src  R-MAT scale 20, 512 sources in one batched launch vs plain
+  pack1024       1,024 R-MAT graphs of scales 10..16 (seed 11), one source
+                 each, in one batched launch vs plain one graph at a time
+The plain R-MAT 22 steps are also checked: two of their sources are re-run
+after the timed loop and compared with the oracle.
+
 Multi-GPU: one process per GPU (torchrun); every rank runs the whole workload
 on its own GPU (replicas: a single SSSP does not shard); value = sum over
 ranks / max time.  ``--impl reference`` times the reference's own CPU code.
@@ -38,6 +51,7 @@ ranks / max time.  ``--impl reference`` times the reference's own CPU code.
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -210,9 +224,12 @@ def cpu_baseline_port(g, srcs, delta, budget_s: float):
                       f"run_sspath_arr (serial), {t_total:.1f} s"}
 
 
-def arm_learned(gb, g, order, W, K):
+def arm_learned(gb, g, order, W, K, par=None):
     from graphbench_gb300 import controller
     g.set_controller(controller.load())
+    if par is not None:   # bit-exact against the plain schedule on the first timed source
+        par.equal("arms", "plain (learned schedule)", g.sssp(order[W], flags=gb.F_LEARNED)[:2],
+                  g.sssp(order[W])[:2])
     for i in range(W):
         g.sssp_device(order[i], flags=gb.F_LEARNED)
     ms = edges = 0.0
@@ -228,10 +245,12 @@ def arm_learned(gb, g, order, W, K):
             "path": "gbs_sssp_device, flags=GBS_F_LEARNED, committed controller block"}
 
 
-def arm_autotuned(gb, g, order, W, K, srcs):
+def arm_autotuned(gb, g, order, W, K, srcs, par=None):
     t0 = time.time()
     kw, rep = g.autotune([int(s) for s in srcs[:4]], budget_ms=3000)
     tune_s = time.time() - t0
+    if par is not None:
+        par.equal("arms", "plain (autotuned schedule)", g.sssp(order[W], **kw)[:2], g.sssp(order[W])[:2])
     for i in range(W):
         g.sssp_device(order[i], **kw)
     ms = edges = 0.0
@@ -244,13 +263,19 @@ def arm_autotuned(gb, g, order, W, K, srcs):
             "delta_scale": rep["delta_scale"], "no_split": rep["no_split"], "tune_seconds": round(tune_s, 1)}
 
 
-def arm_batched(gb, g, srcs, reps: int = 5):
+def arm_batched(gb, g, srcs, reps: int = 5, par=None):
     t0 = time.time()
     bp, rep = gb.autotune_plan(g, srcs, budget_ms=8000)
     tune_s = time.time() - t0
     with gb.Plan(g, srcs, params=bp) as plan:
         for _ in range(2):
             plan.run()
+        if par is not None:
+            ds, ps = plan.results()
+            last = len(srcs) - 1
+            par.equal("arms", "plain (batched instance 0)", (ds[0], ps[0]), g.sssp(int(srcs[0]))[:2])
+            par.equal("arms", f"plain (batched instance {last})", (ds[last], ps[last]), g.sssp(int(srcs[last]))[:2])
+            del ds, ps
         ms = edges = 0.0
         for _ in range(reps):
             st = plan.run()
@@ -360,6 +385,254 @@ def arm_ingest(gb, hg, cpu: bool):
     return out
 
 
+# --------------------------------------------------------------- parity
+def _oracle_check(row, col, w, src, dist, pred):
+    """Bit-for-bit comparison of one GPU result with the oracle: Dijkstra in
+    the weight type and the smallest tight predecessor of every vertex."""
+    import oracle
+    ref = oracle.dijkstra(row, col, w, int(src))
+    dm = int(np.count_nonzero(dist != ref))
+    pm = None
+    if pred is not None:
+        pm = int(np.count_nonzero(pred != oracle.min_tight_pred(row, col, w, int(src), ref)))
+    return {"source": int(src), "dist_mismatches": dm, "pred_mismatches": pm}
+
+
+class Parity:
+    """Oracle checks run in host threads while the GPU carries on (the
+    oracle's C calls release the GIL); collect() waits for them."""
+
+    def __init__(self, workers: int):
+        self.pool = cf.ThreadPoolExecutor(max_workers=max(1, workers))
+        self.jobs: dict[str, list] = {}
+
+    def oracle(self, key: str, hg, src, dist, pred):
+        fut = self.pool.submit(_oracle_check, hg.row, hg.col, hg.w, src, dist, pred)
+        self.jobs.setdefault(key, []).append(fut)
+
+    def equal(self, key: str, what: str, a, b):
+        """A result that must equal another one (learned / autotuned /
+        batched against plain), recorded like an oracle check."""
+        fut = cf.Future()
+        fut.set_result({"compared_with": what, "dist_mismatches": int(np.count_nonzero(a[0] != b[0])),
+                        "pred_mismatches": int(np.count_nonzero(a[1] != b[1]))})
+        self.jobs.setdefault(key, []).append(fut)
+
+    def collect(self, key: str) -> dict:
+        recs = [f.result() for f in self.jobs.pop(key, [])]
+        bad = sum(r["dist_mismatches"] + (r["pred_mismatches"] or 0) for r in recs)
+        return {"result": ("bit-identical" if bad == 0 else "MISMATCH") if recs else "not checked",
+                "checks": recs}
+
+    def close(self):
+        self.pool.shutdown(wait=True)
+
+
+def _timed_runs(g, srcs, reps=1, **kw):
+    """Device-timed single-source runs (CUDA events of the library); returns
+    (GTEPS, ms per run, runs, per-run stats)."""
+    ms = edges = 0.0
+    per = []
+    for _ in range(reps):
+        for s in srcs:
+            st = g.sssp_device(int(s), **kw)
+            ms += st["device_ms"]
+            edges += st["edges_reached"]
+            per.append(st)
+    return edges / ms / 1e6, ms / len(per), len(per), per
+
+
+def _plan_timed(gb, plan, launches):
+    plan.run()
+    ms = edges = 0.0
+    for _ in range(launches):
+        st = plan.run()
+        ms += st["device_ms"]
+        edges += st["edges_reached"]
+    return edges / ms / 1e6, ms / launches, st
+
+
+def config_grid4096(gb, par: Parity, steps: int):
+    """C3: the 4096 x 4096 grid, float32 weights [1, 1000) (seed 3), source 0:
+    plain fixed delta against the autotuned schedule and the learned
+    controller; batching on 8 sources (corner + 7 seeded) of the same grid
+    against those 8 run plain one after another."""
+    from graphbench_gb300 import controller
+    hg = gb.gen_grid(4096, 4096, 3, "f32")
+    out = {"workload": "grid4096_f32", "n": hg.n, "m": hg.m}
+    with gb.Graph.from_host(hg) as g:
+        g.sssp_device(0)
+        v, ms, k, per = _timed_runs(g, [0], reps=max(1, steps))
+        out["plain"] = {"value": v, "unit": "GTEPS", "ms_per_sssp": ms, "runs": k, "phases": per[0]["phases"],
+                        "buckets": per[0]["buckets"], "delta": per[0]["delta_used"]}
+        d0, p0, _ = g.sssp(0)
+        par.oracle("grid4096", hg, 0, d0, p0)
+        t0 = time.time()
+        kw, rep = g.autotune([0], budget_ms=8000)
+        tune_s = time.time() - t0
+        v2, ms2, k2, _ = _timed_runs(g, [0], reps=max(1, steps), **kw)
+        out["autotuned"] = {"value": v2, "unit": "GTEPS", "ms_per_sssp": ms2, "runs": k2, "vs_plain": v2 / v,
+                            "schedule": {a: (round(b, 4) if isinstance(b, float) else b) for a, b in kw.items()},
+                            "tune_seconds": round(tune_s, 1)}
+        par.equal("grid4096", "plain (autotuned schedule)", g.sssp(0, **kw)[:2], (d0, p0))
+        g.set_controller(controller.load())
+        # the first learned call on a graph also times the plain schedule
+        # once (its guard); that run is not part of a learned step
+        g.sssp_device(0, flags=gb.F_LEARNED)
+        lv, lms, lk, lper = _timed_runs(g, [0], reps=max(1, steps), flags=gb.F_LEARNED)
+        out["learned"] = {"value": lv, "unit": "GTEPS", "ms_per_sssp": lms, "runs": lk, "vs_plain": lv / v,
+                          "learned_runs": sum(1 for s in lper if s["learned"] == 1),
+                          "fell_back_runs": sum(1 for s in lper if s["learned"] != 1)}
+        par.equal("grid4096", "plain (learned schedule)", g.sssp(0, flags=gb.F_LEARNED)[:2], (d0, p0))
+        g.set_controller(None)
+        srcs = np.concatenate([[0], gb.sample_sources(hg, 7, 3)]).astype(np.uint32)
+        pv, pms, _, _ = _timed_runs(g, srcs[1:], reps=1)
+        plain8 = (pms * 7 + ms) / 8
+        bp, brep = gb.autotune_plan(g, srcs, budget_ms=8000)
+        with gb.Plan(g, srcs, params=bp) as plan:
+            bv, bms, bst = _plan_timed(gb, plan, 2)
+            ds, ps = plan.results()
+        par.equal("grid4096", "plain (batched instance 0)", (ds[0], ps[0]), (d0, p0))
+        par.oracle("grid4096", hg, int(srcs[7]), ds[7].copy(), ps[7].copy())
+        del ds, ps
+        out["batched"] = {"value": bv, "unit": "GTEPS", "ms_per_launch": bms, "instances": len(srcs),
+                          "plain_ms_for_the_same_sources": plain8 * 8, "vs_plain": (plain8 * 8) / bms,
+                          "groups": bst["groups"], "group_ctas": bst["group_ctas"], "params": brep["best"]}
+    out["parity"] = par.collect("grid4096")
+    return out
+
+
+def config_rmat24(gb, par: Parity, steps: int):
+    """C5: R-MAT scale 24 (edge factor 16, uint32 [1, 255]), 8 sources of seed
+    7: plain, learned, autotuned and batched; every learned / autotuned result
+    compared with the plain one, two plain ones with the oracle."""
+    from graphbench_gb300 import controller
+    hg = gb.gen_rmat(24, 16, 1)
+    srcs = gb.sample_sources(hg, 8, 7)
+    out = {"workload": "rmat24_u32", "n": hg.n, "m": hg.m, "sources": len(srcs)}
+    reps = max(1, steps // len(srcs))
+    with gb.Graph.from_host(hg) as g:
+        for s in srcs[:2]:
+            g.sssp_device(int(s))
+        v, ms, k, per = _timed_runs(g, srcs, reps=reps)
+        out["plain"] = {"value": v, "unit": "GTEPS", "ms_per_sssp": ms, "runs": k,
+                        "avg_phases": sum(p["phases"] for p in per) / k, "delta": per[0]["delta_used"]}
+        ref = {}
+        for s in srcs[:2]:
+            d, p, _ = g.sssp(int(s))
+            ref[int(s)] = (d, p)
+            par.oracle("rmat24", hg, int(s), d, p)
+        g.set_controller(controller.load())
+        g.sssp_device(int(srcs[0]), flags=gb.F_LEARNED)   # the guard's plain timing run
+        lv, lms, lk, lper = _timed_runs(g, srcs, reps=reps, flags=gb.F_LEARNED)
+        out["learned"] = {"value": lv, "unit": "GTEPS", "ms_per_sssp": lms, "runs": lk, "vs_plain": lv / v,
+                          "learned_runs": sum(1 for s in lper if s["learned"] == 1),
+                          "fell_back_runs": sum(1 for s in lper if s["learned"] == 3),
+                          "plain_after_loss_runs": sum(1 for s in lper if s["learned"] == 2)}
+        for s in srcs[:2]:
+            par.equal("rmat24", "plain (learned schedule)", g.sssp(int(s), flags=gb.F_LEARNED)[:2], ref[int(s)])
+        g.set_controller(None)
+        t0 = time.time()
+        kw, rep = g.autotune([int(x) for x in srcs[:2]], budget_ms=4000)
+        tune_s = time.time() - t0
+        av, ams, ak, _ = _timed_runs(g, srcs, reps=reps, **kw)
+        out["autotuned"] = {"value": av, "unit": "GTEPS", "ms_per_sssp": ams, "runs": ak, "vs_plain": av / v,
+                            "schedule": {a: (round(b, 4) if isinstance(b, float) else b) for a, b in kw.items()},
+                            "tune_seconds": round(tune_s, 1)}
+        for s in srcs[:2]:
+            par.equal("rmat24", "plain (autotuned schedule)", g.sssp(int(s), **kw)[:2], ref[int(s)])
+        t0 = time.time()
+        bp, brep = gb.autotune_plan(g, srcs, budget_ms=8000)
+        tune_b = time.time() - t0
+        with gb.Plan(g, srcs, params=bp) as plan:
+            bv, bms, bst = _plan_timed(gb, plan, 2)
+            ds, ps = plan.results()
+        for i in range(2):
+            par.equal("rmat24", f"plain (batched instance {i})", (ds[i], ps[i]), ref[int(srcs[i])])
+        del ds, ps
+        out["batched"] = {"value": bv, "unit": "GTEPS", "ms_per_launch": bms, "instances": len(srcs),
+                          "vs_plain": bv / v, "groups": bst["groups"], "group_ctas": bst["group_ctas"],
+                          "params": brep["best"], "tune_seconds": round(tune_b, 1)}
+    out["parity"] = par.collect("rmat24")
+    return out
+
+
+def config_rmat20_512(gb, par: Parity):
+    """C4a: 512 sources (seed 7) on R-MAT scale 20 in one persistent batched
+    launch replayed from a CUDA graph, against the same 512 run plain one
+    after another; two instances checked with the oracle."""
+    hg = gb.gen_rmat(20, 16, 1)
+    srcs = gb.sample_sources(hg, 512, 7)
+    out = {"workload": "rmat20_512src_u32", "n": hg.n, "m": hg.m, "sources": len(srcs)}
+    with gb.Graph.from_host(hg) as g:
+        for s in srcs[:3]:
+            g.sssp_device(int(s))
+        v, ms, k, _ = _timed_runs(g, srcs)
+        out["plain"] = {"value": v, "unit": "GTEPS", "ms_total": ms * k, "runs": k}
+        t0 = time.time()
+        bp, brep = gb.autotune_plan(g, srcs, budget_ms=6000)
+        tune_b = time.time() - t0
+        with gb.Plan(g, srcs, params=bp) as plan:
+            bv, bms, bst = _plan_timed(gb, plan, 3)
+            ds, ps = plan.results()
+        for i in (0, 511):
+            par.oracle("rmat20_512", hg, int(srcs[i]), ds[i].copy(), ps[i].copy())
+        del ds, ps
+    out["batched"] = {"value": bv, "unit": "GTEPS", "ms_per_launch": bms, "vs_plain": bv / v,
+                      "groups": bst["groups"], "group_ctas": bst["group_ctas"], "params": brep["best"],
+                      "tune_seconds": round(tune_b, 1),
+                      "path": "gbs_plan_sources + gbs_plan_launch (CUDA graph), 512 dist/pred arrays on the device"}
+    out["parity"] = par.collect("rmat20_512")
+    return out
+
+
+def config_pack1024(gb, par: Parity):
+    """C4b: 1,024 independent R-MAT graphs, scales uniform in [10, 16] (seed
+    11), one seeded source each, in one batched launch, against the same
+    graphs run one after another (each its own resident graph, plain
+    schedule); two instances checked with the oracle."""
+    rng = np.random.default_rng(11)
+    scales = rng.integers(10, 17, size=1024)
+    graphs, srcs = [], []
+    for i, sc in enumerate(scales):
+        h = gb.gen_rmat(int(sc), 16, 11 + i)
+        graphs.append(h)
+        srcs.append(int(gb.sample_sources(h, 1, 11 + i)[0]))
+    srcs = np.array(srcs, dtype=np.uint32)
+    out = {"workload": "pack1024_u32", "graphs": len(graphs), "scales": [int(scales.min()), int(scales.max())],
+           "total_n": int(sum(h.n for h in graphs)), "total_m": int(sum(h.m for h in graphs))}
+    ms = edges = 0.0
+    for h, s in zip(graphs, srcs):
+        with gb.Graph.from_host(h) as g:
+            g.sssp_device(int(s))
+            st = g.sssp_device(int(s))
+            ms += st["device_ms"]
+            edges += st["edges_reached"]
+    out["plain"] = {"value": edges / ms / 1e6, "unit": "GTEPS", "ms_total": ms,
+                    "path": "one resident graph and one gbs_sssp_device run per pack graph"}
+    with gb.Pack(graphs) as pk:
+        t0 = time.time()
+        bp, brep = gb.autotune_plan(pk, srcs, budget_ms=6000)
+        tune_b = time.time() - t0
+        with gb.Plan(pk, srcs, params=bp) as plan:
+            bv, bms, bst = _plan_timed(gb, plan, 3)
+            ds, ps = plan.results()
+        big = int(np.argmax([h.m for h in graphs]))
+        for i in (0, big):
+            par.oracle("pack1024", graphs[i], int(srcs[i]), ds[i].copy(), ps[i].copy())
+        del ds, ps
+    out["batched"] = {"value": bv, "unit": "GTEPS", "ms_per_launch": bms, "vs_plain": bv / out["plain"]["value"],
+                      "groups": bst["groups"], "group_ctas": bst["group_ctas"], "params": brep["best"],
+                      "tune_seconds": round(tune_b, 1),
+                      "path": "gbs_pack_create + gbs_plan_pack + gbs_plan_launch (CUDA graph)"}
+    out["parity"] = par.collect("pack1024")
+    return out
+
+
+CONFIGS = {"grid4096_f32": config_grid4096, "rmat24_u32": config_rmat24,
+           "rmat20_512src": config_rmat20_512, "pack1024": config_pack1024}
+
+
 # ----------------------------------------------------------------- our arm
 def run_ours(args):
     world, rank, local = dist_env()
@@ -414,6 +687,13 @@ def run_ours(args):
         _, _, st = g.sssp(order[W + i], delta=delta, light=light, out_dist=hd.array, out_pred=hp.array)
         e2e_t += time.perf_counter() - t
         e2e_edges += st["edges_reached"]
+    # parity of the plain steps: the first two timed sources again, results
+    # to the host, against the oracle (host threads; the GPU carries on)
+    par = Parity(min(8, os.cpu_count() or 1)) if rank == 0 else None
+    if par is not None and not args.no_parity:
+        for src in order[W:W + 2]:
+            d, p, _ = g.sssp(src, delta=delta, light=light)
+            par.oracle("plain", hg, src, d, p)
     # whole-job aggregates
     dev_max = allreduce_max(dist, dev_s)
     wall_max = allreduce_max(dist, wall)
@@ -472,9 +752,9 @@ def run_ours(args):
         }
         if world == 1 and not args.no_arms:
             plain = result["value"]
-            for name, fn in (("learned", lambda: arm_learned(gb, g, order, W, K)),
-                             ("autotuned", lambda: arm_autotuned(gb, g, order, W, K, srcs)),
-                             ("batched", lambda: arm_batched(gb, g, srcs))):
+            for name, fn in (("learned", lambda: arm_learned(gb, g, order, W, K, par)),
+                             ("autotuned", lambda: arm_autotuned(gb, g, order, W, K, srcs, par)),
+                             ("batched", lambda: arm_batched(gb, g, srcs, par=par))):
                 try:
                     arm = fn()
                     arm["vs_plain"] = arm["value"] / plain
@@ -482,12 +762,16 @@ def run_ours(args):
                     arm = {"value": None, "error": str(e)}
                 result[name] = arm
                 log(f"[rank 0] {name}: {arm.get('value')}")
+            result["arms_parity"] = par.collect("arms")
         if world == 1 and not args.no_bc:
             try:
                 result["betweenness"] = arm_betweenness(gb, g, hg, srcs, cpu=not args.no_cpu_baseline)
             except Exception as e:  # pragma: no cover
                 result["betweenness"] = {"value": None, "error": str(e)}
             log(f"[rank 0] betweenness: {result['betweenness'].get('value')}")
+        # the oracle checks of the plain steps finish before the host-bound
+        # ingest measurement starts
+        result["parity"] = par.collect("plain")
         if world == 1 and not args.no_bc:
             for name, fn in (("pagerank", lambda: arm_pagerank(gb, hg, not args.no_cpu_baseline)),
                              ("ingest", lambda: arm_ingest(gb, hg, not args.no_cpu_baseline))):
@@ -506,6 +790,21 @@ def run_ours(args):
     hd.free()
     hp.free()
     g.close()
+    if rank == 0 and world == 1 and args.configs != "none":
+        names = list(CONFIGS) if args.configs == "all" else [c for c in args.configs.split(",") if c]
+        for name in names:
+            t0 = time.time()
+            try:
+                fn = CONFIGS[name]
+                rec = fn(gb, par, args.config_steps) if name in ("grid4096_f32", "rmat24_u32") else fn(gb, par)
+            except Exception as e:  # pragma: no cover
+                rec = {"value": None, "error": f"{type(e).__name__}: {e}"}
+            rec["wall_s"] = round(time.time() - t0, 1)
+            result[name] = rec
+            log(f"[rank 0] {name}: {json.dumps({k: v.get('value') for k, v in rec.items() if isinstance(v, dict) and 'value' in v})} "
+                f"parity {rec.get('parity', {}).get('result')} in {rec['wall_s']} s")
+    if par is not None:
+        par.close()
     if dist is not None:
         dist.destroy_process_group()
     if result is not None:
@@ -523,6 +822,35 @@ def _ref_worker(args_tuple):
     return int(deg[np.isfinite(d)].sum()), secs
 
 
+def _child_call(q, fn, args):
+    try:
+        q.put(("ok", fn(*args)))
+    except BaseException as e:  # pragma: no cover - reported to the parent
+        q.put(("error", f"{type(e).__name__}: {e}"))
+
+
+def _in_child(ctx, fn, args, timeout_s):
+    """fn(*args) in a forked child (the reference keeps globals and never
+    frees, and its OpenMP build can crash): (status, value-or-message)."""
+    q = ctx.Queue()
+    pr = ctx.Process(target=_child_call, args=(q, fn, args))
+    pr.start()
+    try:
+        status, val = q.get(timeout=timeout_s)
+    except Exception:
+        status, val = "error", "no result within the time limit" if pr.is_alive() else f"exit code {pr.exitcode}"
+    pr.join(timeout=5)
+    if pr.is_alive():
+        pr.kill()
+        pr.join()
+    return status, val
+
+
+def _ref_omp(row, col, w, src, delta, maxd, threads):
+    import oracle
+    return oracle.ref_sssp_arr(row, col, w, src, delta, variant="omp", threads=threads, maxdist=maxd, cap_mult=4.0)
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -531,9 +859,13 @@ def run_reference(args):
     import oracle
     from oracle import build_ref, gen
     try:
-        if not oracle.ref_available("serial"):
+        if not (oracle.ref_available("serial") and oracle.ref_available("omp")):
             build_ref.stage()
             build_ref.compile_ref()
+        # mapped in this process before the workers fork, so the process
+        # that prints the line has the compiled reference loaded
+        oracle.ref_lib("serial")
+        oracle.ref_lib("omp")
     except Exception as e:
         print(json.dumps({"impl": "reference", "unavailable": f"reference build failed: {e}"}))
         return
@@ -549,12 +881,15 @@ def run_reference(args):
     row, col, w = gen.rmat(scale, wl["edgefactor"], wl["seed"], wl["wtype"])
     srcs = gen.sample_sources(row, 64, wl["source_seed"])
     delta = gen.heuristic_delta(row, w)
+    exact = {}
     maxd = 0.0
     for s in srcs[:4]:
         dj = oracle.dijkstra(row, col, w, int(s))
+        exact[int(s)] = dj
         maxd = max(maxd, float(dj[dj != 0xFFFFFFFF].max()))
     maxd *= 1.5
-    cores = max(1, min(os.cpu_count() or 1, args.ref_procs))
+    host_cores = os.cpu_count() or 1
+    cores = max(1, min(host_cores, args.ref_procs))
     ctx = mp.get_context("fork")
     K, W = args.steps, args.warmup
     i = 0
@@ -569,7 +904,7 @@ def run_reference(args):
 
     budget = args.ref_budget_s
     with ctx.Pool(cores) as pool:
-        for _ in range(min(W, 1)):
+        for _ in range(W):
             one_step(pool)
         done, edges, secs = 0, 0, 0.0
         t_start = time.perf_counter()
@@ -579,6 +914,29 @@ def run_reference(args):
             secs += s
             done += 1
     val = edges / secs / 1e9
+    # the reference's OpenMP build (-DUSE_OMP), all host cores on one source
+    # at a time; its relax keeps one request per target ordered by edge
+    # weight (structural defect D5), so its distances are counted against
+    # the exact ones
+    deg = np.diff(row.astype(np.int64))
+    omp = {"threads": host_cores, "runs": []}
+    t_omp = 0.0
+    e_omp = 0
+    for s in list(exact)[:4]:
+        st, res = _in_child(ctx, _ref_omp, (row, col, w, s, delta, maxd, host_cores), 120)
+        if st != "ok":
+            omp["runs"].append({"source": s, "status": res})
+            continue
+        d, sec = res
+        ex = exact[s].astype(np.float64)
+        ex[exact[s] == 0xFFFFFFFF] = np.inf
+        omp["runs"].append({"source": s, "seconds": sec, "distance_mismatches": int(np.count_nonzero(d != ex))})
+        t_omp += sec
+        e_omp += int(deg[np.isfinite(ex)].sum())
+    omp["value"] = e_omp / t_omp / 1e9 if t_omp > 0 else None
+    omp["unit"] = "GTEPS"
+    omp["note"] = ("reported beside the serial value, not as it: the OpenMP build is inexact by design "
+                   "(one request per target, ordered by edge weight)")
     sample = (f"{done} step(s) x {cores} concurrent single-source runs of the reference's serial "
               f"run_sspath_arr (patched D1/D2/D4, logging off) on R-MAT scale {scale} (same generator, "
               f"edge factor, weights, delta rule and source seed as {args.workload}); stand-in size because "
@@ -586,11 +944,12 @@ def run_reference(args):
     print(json.dumps({
         "impl": "reference", "metric": "GTEPS SSSP, learned/batched vs plain fixed-delta on 1 GB300; % HBM roofline",
         "value_is": "the reference's serial run_sspath_arr, plain fixed delta", "value": val,
-        "unit": "GTEPS", "n_gpus": world, "steps": done, "warmup": min(W, 1), "ms_per_step": secs * 1e3 / done,
+        "unit": "GTEPS", "n_gpus": world, "steps": done, "warmup": W, "ms_per_step": secs * 1e3 / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference doubles)",
         "data": "synthetic", "config": {"workload": f"{args.workload}_{wl['wtype']}", "reference_scale": scale,
-                                        "delta": delta, "processes": cores},
+                                        "delta": delta, "processes": cores, "host_cores": host_cores},
         "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": cores, "kind": "reference", "sample": sample},
+        "openmp": omp,
         "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -608,6 +967,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-arms", action="store_true", help="skip the learned / autotuned / batched arms")
     ap.add_argument("--no-bc", action="store_true", help="skip the betweenness, PageRank and ingest measurements")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the plain steps")
+    ap.add_argument("--configs", default="all",
+                    help="comma-separated list of " + ", ".join(CONFIGS) + "; 'all' (default) or 'none'")
+    ap.add_argument("--config-steps", type=int, default=2,
+                    help="timed runs per source in the grid4096_f32 / rmat24_u32 records")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-scale", type=int, default=16)
     ap.add_argument("--ref-procs", type=int, default=16)
