@@ -6,26 +6,30 @@ kernel at every bucket start of a ``flags=F_LEARNED`` run (see
 It is trained here, on the GPU, with the library's own CUDA forward, backward
 and Adam kernels (``Mlp``), on traces of the plain method:
 
-1. for each seeded training graph, the autotuner sweeps the bucket width
-   (powers of two times the plain width max_weight / average degree) with and
-   without the light/heavy split and keeps the fastest (``collect_graph``);
-2. fixed-width runs around that best width record the controller inputs at
-   every bucket start (``GBS_F_FEATURES``);
-3. every recorded input is labelled with the graph's best (log2 width
-   scale, split); samples are weighted so that each graph counts once.
-   Every width at or above the largest distance gives the same schedule (one
-   bucket), so the label is capped at the first such width: otherwise small
-   graphs, where every width past that point ties, give labels spread over
-   the whole flat end of the sweep.
-
+1. for each seeded training graph, the plain method runs at every width
+   d * 2^k (k = -2 .. 8, d the plain width max_weight / average degree),
+   with and without the light/heavy split, recording its phase trace and the
+   controller inputs at every bucket start (``collect_graph``);
+2. each run's trace gives the time at which every distance was settled; a
+   recorded bucket start at distance D is labelled with the (k, split) whose
+   run covered the next HORIZON plain widths [D, D + 8 d) fastest.  The
+   controller re-decides at every bucket start, so it learns the width that
+   pays from that point on (narrow where the buckets are large, wide in the
+   sparse tail), not one width per graph.  Samples weigh by the time their
+   window costs at its best width; each graph counts once;
+3. training (``fit``) minimises the squared error of output 0 against k and
+   the logistic loss of output 1 against the split;
 4. the two output biases are calibrated on the held-out graphs
    (``calibrate``): learned runs with output 0 shifted by 0 .. -4 (every
    predicted width divided by up to 16) and output 1 shifted by -30 / 0 / +30
    (always whole rows / as predicted / always split) are timed against the
    plain schedule, and the pair with the best geometric-mean speed-up is
-   added to the block.  The labels are the best FIXED width of a graph, but
-   the controller re-decides at every bucket start, and a width that is best
-   for the whole run is too wide for most buckets taken one at a time.
+   added to the block.
+
+None of the inputs grows with the vertex count by itself (occupancies are
+absolute entry counts, which is what a phase's fixed cost is amortised
+over), so graphs larger than the training ones do not push the network past
+the range of its inputs along the graph size.
 
 Distances never depend on the width, so the controller can only change the
 run time; the library checks that by falling back to the plain schedule when
@@ -92,49 +96,102 @@ def make_graph(spec: dict) -> gb.HostGraph:
     return gb.gen_rmat(spec["scale"], 16, spec["seed"])
 
 
-def collect_graph(spec: dict, tune_budget_ms: float = 800.0, feature_scales=(1 / 8, 1 / 2, 1, 2, 8)) -> dict:
-    """Best plain schedule of one graph and the inputs recorded around it."""
+SWEEP_K = tuple(range(-2, 9))     # log2(width / plain width) of the delta sweep
+HORIZON = 8.0                     # label window, in plain widths
+
+
+def bucket_curve(trace: list[dict], width: float) -> np.ndarray:
+    """(distance start, distance end, time start, time end) of every bucket a
+    fixed-width run processed, from its phase trace (a bucket's time runs from
+    the end of the phase before its first scan to the end of its last phase,
+    so the pending re-bucketing before a bucket counts towards it)."""
+    starts = [i for i, r in enumerate(trace) if r["kind"] == "scan_bucket"]
+    out = []
+    for j, i in enumerate(starts):
+        t0 = trace[i - 1]["end_ns"] if i > 0 else 0
+        last = (starts[j + 1] if j + 1 < len(starts) else len(trace)) - 1
+        b = trace[i]["bucket"]
+        out.append((b * width, (b + 1) * width, t0, trace[last]["end_ns"]))
+    return np.array(out, dtype=np.float64).reshape(-1, 4)
+
+
+def time_at(curve: np.ndarray, dist: np.ndarray) -> np.ndarray:
+    """Time at which a run had finished every distance below dist: linear
+    inside a bucket, flat over distances no bucket held."""
+    d0, d1, t0, t1 = curve.T
+    i = np.searchsorted(d0, dist, side="right") - 1
+    out = np.zeros(len(dist))
+    ok = i >= 0
+    ii = np.clip(i, 0, None)
+    inside = ok & (dist < d1[ii])
+    frac = np.clip((dist - d0[ii]) / np.maximum(d1[ii] - d0[ii], 1e-30), 0.0, 1.0)
+    out[ok] = t1[ii][ok]
+    out[inside] = (t0[ii] + (t1[ii] - t0[ii]) * frac)[inside]
+    return out
+
+
+def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: int = 3000, seed: int = 0) -> dict:
+    """Per-bucket labels from a delta sweep of the plain method on one graph.
+
+    Every width d * 2^k (k in sweep_k, d the plain width) runs with and
+    without the light/heavy split, recording the phase trace and the
+    controller inputs at every bucket start.  Each run gives a curve of time
+    against the distance settled.  A recorded bucket start at distance D gets
+    as label the (k, split) whose run covered [D, D + horizon * d) fastest:
+    the width that pays best from that point of the run on, not one width for
+    the whole graph.  Samples weigh by the time that window costs at its best
+    width, so the expensive stretches of a run count most; a graph's samples
+    weigh 1 in all."""
     host = make_graph(spec)
-    srcs = [0] if spec["kind"] == "grid" else [int(s) for s in gb.sample_sources(host, 2, spec["seed"])]
+    src = 0 if spec["kind"] == "grid" else int(gb.sample_sources(host, 1, spec["seed"])[0])
+    runs = {}
     with gb.Graph.from_host(host) as g:
-        _, rep = g.autotune(srcs, budget_ms=tune_budget_ms)
-        best = float(rep["delta_scale"])
-        split = 0.0 if rep["no_split"] else 1.0
-        d0 = g.info()["default_delta"]
-        d, _, _ = g.sssp(srcs[0], want_pred=False)
-        unreached = np.float32(np.inf) if d.dtype == np.float32 else np.uint32(0xFFFFFFFF)
-        fin = d[d != unreached].astype(np.float64)
-        maxdist = float(fin.max()) if len(fin) else d0
-        one_bucket = 2.0 ** math.ceil(math.log2(max(maxdist / d0, 1.0)))
-        best = min(best, one_bucket)
-        rows = []
-        for f in sorted(set([*feature_scales, 1.0 / best])):
-            light = None if split else math.inf
-            g.sssp(srcs[0], delta=d0 * best * f, light=light, flags=gb.F_FEATURES, want_dist=False,
-                   want_pred=False)
-            x = g.features()
-            if len(x):
-                # the state the host predicts from before bucket 0 (the source
-                # alone in its bucket, nothing done yet), with this run's
-                # graph inputs
-                first = np.concatenate([np.ones(7), np.zeros(4), x[0, 11:]]).astype(np.float32)
-                rows.append(first[None, :])
-            rows.append(x)
-    x = np.concatenate(rows) if rows else np.zeros((0, gb.N_FEAT), np.float32)
-    return {"spec": spec, "best_scale": best, "split": split, "default_ms": rep["default_ms"],
-            "best_ms": rep["best_ms"], "x": x}
+        d = g.info()["default_delta"]
+        g.sssp_device(src)
+        for k in sweep_k:
+            for split in (0, 1):
+                light = None if split else math.inf
+                g.sssp_device(src, delta=d * 2.0 ** k, light=light)          # warm-up
+                st = g.sssp_device(src, delta=d * 2.0 ** k, light=light, flags=gb.F_TRACE | gb.F_FEATURES)
+                tr = g.trace()
+                x = g.features()
+                runs[(k, split)] = (bucket_curve(tr, st["delta_used"]), x, st["kernel_ms"])
+    keys = list(runs)
+    xs, labels, costs = [], [], []
+    for key in keys:
+        curve, x, _ = runs[key]
+        # feature row j belongs to the bucket start j + 1 (bucket 0's width is
+        # the host's first prediction, made before the run)
+        if len(x) != len(curve) - 1 or not len(x):
+            continue
+        dist = curve[1:, 0]
+        h = horizon * d
+        c = np.stack([time_at(runs[q][0], dist + h) - time_at(runs[q][0], dist) for q in keys])
+        best = np.argmin(c, axis=0)
+        xs.append(x)
+        labels.append(np.array([[keys[b][0], keys[b][1]] for b in best], dtype=np.float32))
+        costs.append(c[best, np.arange(len(best))])
+    if not xs:
+        return {"spec": spec, "x": np.zeros((0, gb.N_FEAT), np.float32), "t": np.zeros((0, 2), np.float32),
+                "w": np.zeros(0, np.float32), "best_fixed": None}
+    x = np.concatenate(xs)
+    t = np.concatenate(labels)
+    w = np.concatenate(costs) + 1e-3
+    if len(x) > cap:
+        keep = np.random.default_rng(seed).choice(len(x), cap, replace=False)
+        x, t, w = x[keep], t[keep], w[keep]
+    total = {q: runs[q][2] for q in keys}
+    best_fixed = min(total, key=total.get)
+    return {"spec": spec, "x": x.astype(np.float32), "t": t, "w": (w / w.sum()).astype(np.float32),
+            "best_fixed": {"k": best_fixed[0], "split": best_fixed[1], "ms": total[best_fixed],
+                           "plain_ms": total[(0, 1)]}}
 
 
 def dataset(collected: list[dict]):
-    """(inputs, targets, weights) with every graph's samples weighing 1 in all."""
-    xs, ts, ws = [], [], []
-    for c in collected:
-        k = len(c["x"])
-        if not k:
-            continue
-        xs.append(c["x"])
-        ts.append(np.tile([math.log2(c["best_scale"]), c["split"]], (k, 1)))
-        ws.append(np.full(k, 1.0 / k))
+    """(inputs, targets, weights); every graph's samples weigh 1 in all."""
+    xs = [c["x"] for c in collected if len(c["x"])]
+    ts = [c["t"] for c in collected if len(c["x"])]
+    ws = [c["w"] for c in collected if len(c["x"])]
     return (np.concatenate(xs).astype(np.float32), np.concatenate(ts).astype(np.float32),
             np.concatenate(ws).astype(np.float32))
 
@@ -235,11 +292,11 @@ def main(argv=None) -> int:
         return 0
     collected = []
     for i, s in enumerate(specs):
-        c = collect_graph(s, tune_budget_ms=8000.0 if s["kind"] == "grid" else 800.0)
+        c = collect_graph(s, seed=i)
         collected.append(c)
-        print(json.dumps({"i": i, **s, "best_scale": c["best_scale"], "split": c["split"],
-                          "samples": len(c["x"]), "default_ms": round(c["default_ms"], 3),
-                          "best_ms": round(c["best_ms"], 3)}), flush=True)
+        print(json.dumps({"i": i, **s, "samples": len(c["x"]), "best_fixed": c["best_fixed"],
+                          "label_k_mean": round(float(np.average(c["t"][:, 0], weights=c["w"])), 2)
+                          if len(c["x"]) else None}), flush=True)
     # every tenth graph is held out for validation
     tr = [c for i, c in enumerate(collected) if i % 10 != 9]
     va = [c for i, c in enumerate(collected) if i % 10 == 9]
@@ -252,8 +309,8 @@ def main(argv=None) -> int:
     summary = {"graphs": len(specs), "samples": int(len(x)), "train_loss_first": float(losses[0]),
                "train_loss_last": float(losses[-1]), "val_loss": float(vloss), "calibration": cal,
                "seconds": round(time.time() - t0, 1),
-               "per_graph": [{**c["spec"], "best_scale": c["best_scale"], "split": c["split"],
-                              "default_ms": c["default_ms"], "best_ms": c["best_ms"]} for c in collected]}
+               "per_graph": [{**c["spec"], "samples": int(len(c["x"])), "best_fixed": c["best_fixed"]}
+                             for c in collected]}
     if args.summary:
         Path(args.summary).write_text(json.dumps(summary, indent=1))
     print(json.dumps({k: v for k, v in summary.items() if k != "per_graph"}), flush=True)

@@ -437,7 +437,11 @@ float mlp_host(const float *P, const float (&x)[kFeat], float &y1) {
     return y0;
 }
 
-// Graph features 11..14 of the controller input (15 is set per run).
+// Graph inputs of the controller: f[1..3] are inputs 12..14 (average
+// degree, largest weight, mean / largest weight), f[4] (input 15, the base
+// width over the plain one) is set per run.  f[0] (log2 of the vertex count)
+// is kept for reports only: the network sees no input that grows with the
+// graph by itself, so it does not extrapolate along the graph size.
 void graph_features(const gbs_graph *g, float *f) {
     const double avg = g->n ? (double)g->m / (double)g->n : 0.0;
     f[0] = (float)std::log2((double)std::max<uint32_t>(g->n, 1));
@@ -461,18 +465,19 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dis
     if (learned) {
         // the controller's first prediction (bucket 0 holds only the source),
         // clamped to the range the training labels cover, fixes the base
-        // width: half the predicted delta, so spans of 1..64 base widths reach
-        // 2x below and 32x above it and the ring window holds 32 predicted
-        // widths; the split is at the predicted delta
+        // width: an eighth of the predicted delta, so spans of 1..64 base
+        // widths reach 8x below and 8x above it (later buckets, far larger
+        // than the source's, usually want narrower ones); the split is at
+        // the predicted delta
         float x[kFeat];
         for (int i = 0; i < 7; ++i) x[i] = 1.f;
-        for (int i = 7; i < 11; ++i) x[i] = 0.f;
-        for (int i = 0; i < 4; ++i) x[11 + i] = gfeat[i];
+        for (int i = 7; i < 12; ++i) x[i] = 0.f;   // 11: the source is the whole window
+        for (int i = 1; i < 4; ++i) x[11 + i] = gfeat[i];
         x[15] = 0.f;
         float y1 = 0.f;
         const float y0 = mlp_host(g->mlp_host.data(), x, y1);
         const double p0 = std::rint(std::min(std::max((double)y0, -2.0), 14.0));
-        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 1.0), d_def * std::exp2(p0));
+        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 3.0), d_def * std::exp2(p0));
         span_bias = (float)std::log2(d_def / r.delta);
         int e0 = (int)std::rint(y0 + span_bias);
         e0 = std::min(std::max(e0, 0), (int)kMaxSpanLog);

@@ -204,7 +204,7 @@ struct SsspArgs {
     uint32_t span_fixed;    // kCtrlFixed: base widths per bucket (0 or 1 = plain delta-stepping)
     float span_bias;        // kCtrlLearned: span = 2^clamp(round(y0 + span_bias), 0, kMaxSpanLog)
     const float *mlp;       // kCtrlLearned: parameter block (kMlpFloats)
-    float gfeat[5];         // graph features 11..15 of the controller input
+    float gfeat[5];         // graph inputs 12..15 of the controller are gfeat[1..4] (see graph_features)
     unsigned long long guard_ns;   // kCtrlLearned: stop with kErrGuard past this run time (0 = none)
     float *feat;            // GBS_F_FEATURES: kFeat floats per bucket start
     uint32_t feat_cap;

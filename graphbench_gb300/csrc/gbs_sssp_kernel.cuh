@@ -205,6 +205,10 @@ __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t
             const uint32_t pos = (q[j] < 32 ? x0 : q[j] < 64 ? x1 : x2) + rank[j];
             if (pos < n) queue_list(a, t, q[j])[pos] = v[j];
             else atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
+            // a pending entry may be re-bucketed by the very next phase, on
+            // this CTA alone, which reads the list from L2 after nothing but
+            // __syncthreads: the store must have reached L2 first
+            if (q[j] == kNB + 1) __threadfence();
         }
     }
     __syncwarp();
@@ -282,6 +286,10 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
         } else if (kind[j] == 3u) {
             atomicMin(&a.ws.ctl->pend_min[t.pend_sel].v, nb[j]);
             r[j] = atomicMin(a.ws.tag + v[j], kTagPending);
+            // the pending minimum steers the next decision; a phase run by
+            // one CTA reaches that decision through __syncthreads alone,
+            // which does not wait for a reduction whose result is unused
+            __threadfence();
         }
     }
 #pragma unroll

@@ -303,6 +303,11 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
         }
         warp_enqueue<1>(a, t, q, v);
     }
+    // the tags just stored and the pending minimum feed the next decision and
+    // the next scan; on one CTA only __syncthreads separates them from this
+    // phase, and it waits neither for the plain stores to reach L2 (where the
+    // scan's L2-only loads read) nor for the reduction
+    __threadfence();
     // entries that had already left the pending list (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) stale += __shfl_down_sync(0xffffffffu, stale, o);
     if (lane_id() == 0 && stale) atomicAdd(&ctl->edge_cnt.v, stale);
@@ -509,11 +514,16 @@ __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint3
         f[5] = __log2f(1.f + first(32));
         f[6] = __log2f(1.f + first(32) + (float)hi_sum);
         f[7] = __log2f(1.f + (float)pend);
-        f[8] = __log2f(1.f + (float)nb);
+        // the distance reached, in plain widths (the base width is
+        // 2^gfeat[4] plain widths)
+        f[8] = __log2f(1.f + (float)nb * exp2f(a.gfeat[4]));
         f[9] = __log2f(1.f + (float)st_b);
         f[10] = __log2f(1.f + (float)st_p);
+        // share of the window's entries in the next base bucket (<= 0): none
+        // of the inputs grows with the vertex count by itself
+        f[11] = f[0] - f[6];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) f[11 + i] = a.gfeat[i];
+        for (int i = 1; i < 5; ++i) f[11 + i] = a.gfeat[i];
         if (want_feat && lane == 0) {
             const uint32_t fi = ctl->feat_n;
             if (fi < a.feat_cap) {
@@ -706,11 +716,10 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         case kPhPending: items = ps2 ? pc1 : pc0; break;
         default: break;
     }
-    // re-bucketing always runs on the grid: run on one CTA it lost survivors
-    // (measured; cause not yet understood), and it happens a few times per run.
-    // INIT and FINISH (batched launches) always run on the whole group.
-    solo = next < kPhDone && next != kPhPending &&
-           (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
+    // INIT and FINISH (batched launches) always run on the whole group; a
+    // small re-bucketing of the pending list runs on this CTA like any small
+    // scan
+    solo = next < kPhDone && (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
     if (lane == 0) {
         if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
             const uint32_t ti = ctl->trace_n;
@@ -868,7 +877,21 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             const bool solo = s_flag[1] != 0;
             __syncthreads();
             if (!solo) break;
+            // A re-bucketing of the pending list on this CTA is fenced by
+            // every thread on both sides: the phases before it wrote the
+            // entries, tags and distances it reads, and the decision after it
+            // reads the ring and pending counters it fills.  Without both
+            // fences 200 of 432 small-width runs (grids and R-MATs, widths
+            // 1-20) lost vertices or stopped early; fences inside the
+            // re-bucketing and after each pending push alone were not enough
+            // (measured).  The phase is rare (a few per run at most on the
+            // published configurations).
+            if (U.phase == kPhPending) {
+                __threadfence();
+                __syncthreads();
+            }
             run_phase<WT>(a, U, cta_exec(), scr, imp);
+            if (U.phase == kPhPending) __threadfence();
             // the decision is taken by this CTA: __syncthreads makes every
             // global access of the phase (the fire-and-forget tag and pend_min
             // reductions included) visible to all its threads, as it does for

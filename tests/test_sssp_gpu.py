@@ -117,6 +117,12 @@ def test_solo_phases_same_result(mode, gb, orc):
     _, _, st2 = run_and_check(gb, orc, g2.row, g2.col, g2.w, 0, **kw)
     if mode == "default":
         assert st2["solo_phases"] > 0
+    # pending traffic (weights up to 255, width 2): the re-bucketing of the
+    # pending list runs on one CTA in the solo modes
+    g3 = gb.gen_grid(60, 90, 11, "u32")
+    for src in (0, 2777):
+        _, _, st3 = run_and_check(gb, orc, g3.row, g3.col, g3.w, src, delta=2, **kw)
+        assert st3["pending_scans"] >= 1
 
 
 @pytest.mark.parametrize("full_items", [1, 0, 1 << 30])
@@ -179,6 +185,25 @@ def test_pending_list_small_delta(gb, orc):
     a = gb.gen_grid(40, 60, 11, "u32")
     _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, 0, delta=1)
     assert st["pending_scans"] >= 1
+
+
+@pytest.mark.parametrize("mode", ["default", "all_solo"])
+def test_pending_rebucketing_on_one_cta(mode, gb, orc):
+    """Widths far below the largest weight push most vertices past the ring
+    window; their re-bucketing runs on the deciding CTA when the pending list
+    is small.  Every run must give the oracle's distances and predecessors
+    (before the re-bucketing fenced its tag stores and the pending minimum,
+    half of these runs on one CTA stopped early or skipped vertices)."""
+    kw = {} if mode == "default" else dict(solo_entries=1 << 30, solo_descs=1 << 30)
+    cases = [(gb.gen_grid(54, 83, 107, "u32"), [1, 2, 3]), (gb.gen_grid(47, 71, 205, "f32"), [2.0, 20.0]),
+             (gb.gen_rmat(12, 16, 302), [1, 4])]
+    pend = 0
+    for a, deltas in cases:
+        for src in [int(x) for x in gb.sample_sources(a, 2, 5)]:
+            for d in deltas:
+                _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, delta=d, **kw)
+                pend += st["pending_scans"]
+    assert pend > 20
 
 
 @pytest.mark.parametrize("delta", [None, 50.0, 1000.0, 1e6])
