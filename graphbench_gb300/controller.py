@@ -10,9 +10,13 @@ and Adam kernels (``Mlp``), on traces of the plain method:
    d * 2^k (k = -2 .. 8, d the plain width max_weight / average degree),
    with and without the light/heavy split, recording its phase trace and the
    controller inputs at every bucket start (``collect_graph``);
-2. each run's trace gives the time at which every distance was settled; a
-   recorded bucket start at distance D is labelled with the (k, split) whose
-   run covered the next HORIZON plain widths [D, D + 8 d) fastest.  The
+2. each run's trace gives the time at which every distance was settled
+   (inside a bucket, its time is spread over the vertices it settles, whose
+   final distances every schedule shares); a recorded bucket start at
+   distance D is labelled with the (k, split) whose run covered the next
+   HORIZON plain widths [D, D + 8 d) fastest.  The initial state (the source
+   alone; the host predicts the run's base width from it) is labelled with
+   the graph's best fixed (k, split) and carries the vertex count.  The
    controller re-decides at every bucket start, so it learns the width that
    pays from that point on (narrow where the buckets are large, wide in the
    sparse tail), not one width per graph.  Samples weigh by the time their
@@ -115,19 +119,40 @@ def bucket_curve(trace: list[dict], width: float) -> np.ndarray:
     return np.array(out, dtype=np.float64).reshape(-1, 4)
 
 
-def time_at(curve: np.ndarray, dist: np.ndarray) -> np.ndarray:
-    """Time at which a run had finished every distance below dist: linear
-    inside a bucket, flat over distances no bucket held."""
+def time_at(curve: np.ndarray, dist: np.ndarray, settled=None) -> np.ndarray:
+    """Time at which a run had finished every distance below dist, flat over
+    distances no bucket held.  Inside a bucket the time is spread over the
+    vertices it settles: settled(D) counts the vertices whose final distance
+    is below D (the same for every schedule), so a wide bucket is charged in
+    a window in proportion to the vertices that window holds, not to its
+    width (uniform spreading when settled is None)."""
     d0, d1, t0, t1 = curve.T
     i = np.searchsorted(d0, dist, side="right") - 1
     out = np.zeros(len(dist))
     ok = i >= 0
     ii = np.clip(i, 0, None)
     inside = ok & (dist < d1[ii])
-    frac = np.clip((dist - d0[ii]) / np.maximum(d1[ii] - d0[ii], 1e-30), 0.0, 1.0)
+    if settled is None:
+        frac = np.clip((dist - d0[ii]) / np.maximum(d1[ii] - d0[ii], 1e-30), 0.0, 1.0)
+    else:
+        lo, hi = settled(d0[ii]), settled(d1[ii])
+        frac = np.clip((settled(dist) - lo) / np.maximum(hi - lo, 1.0), 0.0, 1.0)
     out[ok] = t1[ii][ok]
     out[inside] = (t0[ii] + (t1[ii] - t0[ii]) * frac)[inside]
     return out
+
+
+def initial_input(n: int, gfeat) -> np.ndarray:
+    """The controller input the host predicts the run's base width from,
+    before bucket 0 (the source alone in the window): the window entries
+    input (6) carries log2(1 + n), the vertices the run will settle, so the
+    base width can follow the graph's size; the kernel's own inputs at later
+    bucket starts grow with no size by themselves."""
+    x = np.zeros(gb.N_FEAT, np.float32)
+    x[0:6] = 1.0
+    x[6] = math.log2(1.0 + n)
+    x[12:15] = gfeat
+    return x
 
 
 def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: int = 3000, seed: int = 0) -> dict:
@@ -147,6 +172,10 @@ def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: in
     runs = {}
     with gb.Graph.from_host(host) as g:
         d = g.info()["default_delta"]
+        fin, _, _ = g.sssp(src, want_pred=False)
+        fin = fin[fin != np.uint32(0xFFFFFFFF)] if fin.dtype == np.uint32 else fin[np.isfinite(fin)]
+        fin = np.sort(fin.astype(np.float64))
+        settled = lambda dd: np.searchsorted(fin, dd, side="left").astype(np.float64)
         g.sssp_device(src)
         for k in sweep_k:
             for split in (0, 1):
@@ -166,7 +195,7 @@ def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: in
             continue
         dist = curve[1:, 0]
         h = horizon * d
-        c = np.stack([time_at(runs[q][0], dist + h) - time_at(runs[q][0], dist) for q in keys])
+        c = np.stack([time_at(runs[q][0], dist + h, settled) - time_at(runs[q][0], dist, settled) for q in keys])
         best = np.argmin(c, axis=0)
         xs.append(x)
         labels.append(np.array([[keys[b][0], keys[b][1]] for b in best], dtype=np.float32))
@@ -182,6 +211,18 @@ def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: in
         x, t, w = x[keep], t[keep], w[keep]
     total = {q: runs[q][2] for q in keys}
     best_fixed = min(total, key=total.get)
+    # the initial state, labelled with the graph's best fixed schedule: the
+    # base width the host derives from it bounds every later bucket's
+    # width to 1/8 .. 8x of that prediction; it weighs as much as all the
+    # graph's bucket starts together
+    avg = host.m / max(host.n, 1)
+    wmax = float(host.w.max()) if host.m else 1.0
+    gfeat = [math.log2(max(avg, 1e-3)), math.log2(max(wmax, 1e-30)),
+             float(host.w.astype(np.float64).mean() / wmax) if host.m else 0.0]
+    x0 = initial_input(host.n, gfeat)[None, :]
+    x = np.concatenate([x0, x])
+    t = np.concatenate([np.array([[best_fixed[0], best_fixed[1]]], np.float32), t])
+    w = np.concatenate([[1.0], w / w.sum()])
     return {"spec": spec, "x": x.astype(np.float32), "t": t, "w": (w / w.sum()).astype(np.float32),
             "best_fixed": {"k": best_fixed[0], "split": best_fixed[1], "ms": total[best_fixed],
                            "plain_ms": total[(0, 1)]}}

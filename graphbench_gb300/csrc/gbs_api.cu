@@ -465,22 +465,29 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dis
     if (learned) {
         // the controller's first prediction (bucket 0 holds only the source),
         // clamped to the range the training labels cover, fixes the base
-        // width: an eighth of the predicted delta, so spans of 1..64 base
-        // widths reach 8x below and 8x above it (later buckets, far larger
-        // than the source's, usually want narrower ones); the split is at
-        // the predicted delta
+        // width: half the predicted delta, so spans of 1..8 base widths reach
+        // 2x below and 4x above it; the split is at the predicted delta.
+        // (Measured with the same trained block: spans of up to 64 base
+        // widths of an eighth of the prediction let the per-bucket outputs
+        // run 4-16x wide on R-MAT 22 / 24, 0.49x / 0.29x of plain; up to 8
+        // of a half, 0.92x / 0.83x, and the grids and smaller R-MATs gain.)
+        // input: the source alone in the window, whose entries input (6)
+        // carries log2(1 + n), the vertices the run will settle (the
+        // controller's training pipeline encodes the initial state the same
+        // way), and the graph inputs
         float x[kFeat];
-        for (int i = 0; i < 7; ++i) x[i] = 1.f;
-        for (int i = 7; i < 12; ++i) x[i] = 0.f;   // 11: the source is the whole window
+        for (int i = 0; i < 6; ++i) x[i] = 1.f;
+        x[6] = (float)std::log2(1.0 + (double)g->n);
+        for (int i = 7; i < 12; ++i) x[i] = 0.f;
         for (int i = 1; i < 4; ++i) x[11 + i] = gfeat[i];
         x[15] = 0.f;
         float y1 = 0.f;
         const float y0 = mlp_host(g->mlp_host.data(), x, y1);
         const double p0 = std::rint(std::min(std::max((double)y0, -2.0), 14.0));
-        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 3.0), d_def * std::exp2(p0));
+        r = resolve_schedule(g->wtype, g->max_w, g->n, g->m, d_def * std::exp2(p0 - 1.0), d_def * std::exp2(p0));
         span_bias = (float)std::log2(d_def / r.delta);
         int e0 = (int)std::rint(y0 + span_bias);
-        e0 = std::min(std::max(e0, 0), (int)kMaxSpanLog);
+        e0 = std::min(std::max(e0, 0), (int)kLearnedSpanLog);
         span0 = 1u << e0;
         full0 = y1 <= 0.f ? 1u : 0u;
     } else {
@@ -887,7 +894,7 @@ gbs_status gbs_graph_set_controller(gbs_graph *g, const float *params, uint32_t 
     if (!g->d_mlp) GBS_CUDA(cudaMalloc(&g->d_mlp, sizeof(float) * kMlpFloats));
     GBS_CUDA(cudaMemcpy(g->d_mlp, params, sizeof(float) * kMlpFloats, cudaMemcpyHostToDevice));
     g->mlp_host.assign(params, params + kMlpFloats);
-    g->ctrl_margin = margin > 0 ? margin : 0.25;
+    g->ctrl_margin = margin > 0 ? margin : 0.10;
     g->plain_ms = 0.0;
     g->ctrl_lost = false;
     return GBS_OK;

@@ -65,6 +65,7 @@ constexpr int kMlpB3 = kMlpW3 + kHid * 2;
 constexpr int kMlpFloats = kMlpB3 + 2;
 constexpr int kMlpParams = kMlpFloats - 2 * kFeat;   // trained parameters (5,378)
 constexpr uint32_t kMaxSpanLog = 6;                  // a bucket spans at most 2^6 = kNB base widths
+constexpr uint32_t kLearnedSpanLog = 3;              // a learned bucket spans at most 2^3 base widths
 
 // One record per grid phase when GBS_F_TRACE is set (layout = gbs_phase_rec).
 struct TraceRec {
@@ -202,7 +203,7 @@ struct SsspArgs {
     // bucket-width controller
     uint32_t ctrl;          // CtrlMode
     uint32_t span_fixed;    // kCtrlFixed: base widths per bucket (0 or 1 = plain delta-stepping)
-    float span_bias;        // kCtrlLearned: span = 2^clamp(round(y0 + span_bias), 0, kMaxSpanLog)
+    float span_bias;        // kCtrlLearned: span = 2^clamp(round(y0 + span_bias), 0, kLearnedSpanLog)
     const float *mlp;       // kCtrlLearned: parameter block (kMlpFloats)
     float gfeat[5];         // graph inputs 12..15 of the controller are gfeat[1..4] (see graph_features)
     unsigned long long guard_ns;   // kCtrlLearned: stop with kErrGuard past this run time (0 = none)

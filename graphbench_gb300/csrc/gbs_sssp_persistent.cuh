@@ -536,7 +536,7 @@ __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint3
             float y0, y1;
             mlp_eval(a.mlp, f, y0, y1);
             int e = (int)rintf(y0 + a.span_bias);
-            e = e < 0 ? 0 : (e > (int)kMaxSpanLog ? (int)kMaxSpanLog : e);
+            e = e < 0 ? 0 : (e > (int)kLearnedSpanLog ? (int)kLearnedSpanLog : e);
             span = 1u << e;
             full = (a.no_heavy || y1 <= 0.f) ? 1u : 0u;   // y1: logit of "split at the light bound"
         }

@@ -334,9 +334,9 @@ gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *c
  * warp at every bucket start of a GBS_F_LEARNED run: output 0 predicts
  * log2(delta / default delta), output 1 is the logit of "split light/heavy at
  * the predicted delta" (else every edge is light).  The run's base width is
- * an eighth of the width predicted for the first bucket (that prediction
- * clamped to 2^-2 .. 2^14 times the default); each bucket spans 2^k base
- * widths (k in 0..6) as output 0 says.  Inputs: log2(1 + entries) of the
+ * half the width predicted for the first bucket (that prediction clamped to
+ * 2^-2 .. 2^14 times the default); each bucket spans 2^k base widths (k in
+ * 0..3) as output 0 says.  Inputs: log2(1 + entries) of the
  * first 1, 2, 4, .., 32 base buckets from the bucket start and of the whole
  * window (7 inputs), log2(1 + pending), log2(1 + distance reached in default
  * widths), log2(1 + buckets done), log2(1 + phases done), the log2 share of
@@ -345,7 +345,7 @@ gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *c
  * None of them grows with the vertex count by itself.
  * params: 5410 floats: input means[16], input scales[16], W1[16][64], b1[64],
  * W2[64][64], b2[64], W3[64][2], b3[2] (row-major, inputs first).  margin
- * (<= 0: 0.25): a learned run that runs longer than (1 + margin) times the
+ * (<= 0: 0.10): a learned run that runs longer than (1 + margin) times the
  * plain schedule on this graph stops and the plain schedule runs instead.  If
  * that plain run finished within the limit (5% timing noise allowed), the
  * controller lost: from then on GBS_F_LEARNED calls on the graph run the plain

@@ -43,6 +43,25 @@ def test_committed_controller_block(gb):
     assert np.all(np.isfinite(p)) and np.all(p[16:32] > 0)
 
 
+def test_label_curve_spreads_bucket_time_over_settled_vertices(gb):
+    """The per-bucket labels compare schedules by the time each needs to
+    settle a window of distances: a bucket's time is spread over the
+    vertices it settles (their final distances are the same for every
+    schedule), and flat over distances no bucket held."""
+    from graphbench_gb300 import controller as c
+    trace = [{"kind": "scan_bucket", "bucket": 0, "end_ns": 10}, {"kind": "relax", "bucket": 0, "end_ns": 20},
+             {"kind": "scan_bucket", "bucket": 1, "end_ns": 30}, {"kind": "scan_light", "bucket": 1, "end_ns": 40},
+             {"kind": "scan_bucket", "bucket": 4, "end_ns": 55}]
+    curve = c.bucket_curve(trace, 2.0)
+    assert curve.tolist() == [[0, 2, 0, 20], [2, 4, 20, 40], [8, 10, 40, 55]]
+    fin = np.array([0.0, 0.5, 0.6, 2.5, 3.9, 9.0])
+    settled = lambda d: np.searchsorted(fin, d, side="left").astype(np.float64)
+    t = c.time_at(curve, np.array([0.0, 0.55, 1.0, 3.0, 5.0, 8.5, 20.0]), settled)
+    assert np.allclose(t, [0.0, 20 * 2 / 3, 20.0, 30.0, 40.0, 40.0, 55.0])
+    x0 = c.initial_input(1023, [4.0, 8.0, 0.5])
+    assert x0[6] == 10.0 and np.all(x0[:6] == 1) and np.all(x0[7:12] == 0) and x0[15] == 0
+
+
 @pytest.mark.gpu
 def test_cuda_loss_and_gradient_match_oracle(gb):
     x, t, w = _data(1000, 2)
@@ -130,7 +149,8 @@ def test_feature_recording(gb):
 @pytest.mark.gpu
 def test_learned_guard_falls_back_to_plain(gb, orc):
     """A controller that always asks for the finest width it may (1/8 of the
-    plain one) on a grid, where wide buckets pay: the learned run passes its
+    plain one: half of its clamped first prediction, 2^-2) on a grid,
+    where wide buckets pay: the learned run passes its
     guard ((1 + margin) x the plain time), stops, and the plain schedule gives
     the result."""
     from graphbench_gb300 import controller
@@ -178,10 +198,12 @@ def test_learned_guard_longer_source_is_not_a_loss(gb, orc):
 
 @pytest.mark.gpu
 def test_trained_controller_beats_plain_on_held_out_graphs(gb):
-    """The committed controller on graphs and seeds outside its training set:
-    total kernel time of learned runs below the plain fixed delta's (a call
-    whose learned run fell back is charged both runs)."""
-    cases = [(gb.gen_grid(768, 768, 97, "f32"), [0]), (gb.gen_rmat(18, 16, 77), None)]
+    """The committed controller on graphs and seeds outside its training set
+    (a 768^2 grid, R-MAT 18 and R-MAT 20, the largest training scale): total
+    kernel time of learned runs below the plain fixed delta's (a call whose
+    learned run fell back is charged both runs)."""
+    cases = [(gb.gen_grid(768, 768, 97, "f32"), [0]), (gb.gen_rmat(18, 16, 77), None),
+             (gb.gen_rmat(20, 16, 5), None)]
     for host, srcs in cases:
         srcs = srcs if srcs is not None else [int(s) for s in gb.sample_sources(host, 6, 5)]
         with _learned_graph(gb, host) as g:
