@@ -24,6 +24,7 @@
 //             round, written by the light scans, relaxed by HEAVY
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -125,6 +126,41 @@ struct __align__(128) Ctl {
     unsigned long long inst_t0;   // globaltimer when the current instance started
 };
 static_assert(sizeof(Ctl) % 128 == 0, "Ctl lines");
+
+// The list counters of Ctl (ring_cnt .. edge_cnt, consecutive Lines) by
+// index.  A phase run by the whole grid reaches them in global memory, one
+// Line apart; the deciding CTA keeps a copy in its shared memory while it
+// decides and while it runs phases alone, one word apart, and writes it back
+// before it releases the other CTAs.  Four statistics words follow the
+// counters in the shared copy (their global homes are the st_* fields).
+enum CtrIdx : uint32_t {
+    kCRing = 0,
+    kCFq = kNB,
+    kCHdesc = kNB + 3,
+    kCPend = kNB + 4,
+    kCPmin = kNB + 6,
+    kCDesc = kNB + 8,
+    kCEdge = kNB + 9,
+    kCtrWords = kNB + 10,
+    kSPhases = kCtrWords,
+    kSBuckets,
+    kSPending,
+    kSSolo,
+    kCtrShared,
+};
+static_assert(offsetof(Ctl, fq_cnt) == offsetof(Ctl, ring_cnt) + 128 * kCFq, "counter order");
+static_assert(offsetof(Ctl, hdesc_cnt) == offsetof(Ctl, ring_cnt) + 128 * kCHdesc, "counter order");
+static_assert(offsetof(Ctl, pend_cnt) == offsetof(Ctl, ring_cnt) + 128 * kCPend, "counter order");
+static_assert(offsetof(Ctl, pend_min) == offsetof(Ctl, ring_cnt) + 128 * kCPmin, "counter order");
+static_assert(offsetof(Ctl, desc_cnt) == offsetof(Ctl, ring_cnt) + 128 * kCDesc, "counter order");
+static_assert(offsetof(Ctl, edge_cnt) == offsetof(Ctl, ring_cnt) + 128 * kCEdge, "counter order");
+
+// Where a phase's list counters live: counter i at base + i * stride.
+struct Ctrs {
+    uint32_t *base;
+    uint32_t stride;   // 32 words (global Lines) or 1 (shared copy)
+    __device__ __forceinline__ uint32_t *at(uint32_t i) const { return base + i * stride; }
+};
 
 struct DevGraph {
     uint32_t n;
@@ -233,6 +269,12 @@ __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
     uint32_t v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// The same load through a generic address (a counter in global or shared memory).
+__device__ __forceinline__ uint32_t ld_relaxed_any(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 // Barrier arrival: release (this CTA's phase, made visible to thread 0 by

@@ -151,14 +151,14 @@ struct Targets {
     uint32_t fq_next;     // index of the next-frontier list
     uint32_t pend_sel;    // pending list to append to
     WarpScratch *scr;     // this warp's shared-memory scratch
+    Ctrs c;               // the list counters (global, or the deciding CTA's shared copy)
 };
 
 // Queue ids: -1 none, 0 next frontier, 1..kNB ring slots, kNB+1 pending.
-__device__ __forceinline__ uint32_t *queue_counter(const SsspArgs &a, const Targets &t, int q) {
-    Ctl *ctl = a.ws.ctl;
-    if (q == 0) return &ctl->fq_cnt[t.fq_next].v;
-    if (q <= kNB) return &ctl->ring_cnt[q - 1].v;
-    return &ctl->pend_cnt[t.pend_sel].v;
+__device__ __forceinline__ uint32_t *queue_counter(const Targets &t, int q) {
+    if (q == 0) return t.c.at(kCFq + t.fq_next);
+    if (q <= kNB) return t.c.at(kCRing + (uint32_t)(q - 1));
+    return t.c.at(kCPend + t.pend_sel);
 }
 __device__ __forceinline__ uint32_t *queue_list(const SsspArgs &a, const Targets &t, int q) {
     const size_t n = a.g.n;
@@ -191,9 +191,9 @@ __device__ __forceinline__ void warp_enqueue(const SsspArgs &a, const Targets &t
     __syncwarp();
     const int i0 = (int)lane, i1 = (int)lane + 32, i2 = (int)lane + 64;
     const uint32_t c0 = cnt[i0], c1 = cnt[i1], c2 = i2 < kQueues ? cnt[i2] : 0u;
-    const uint32_t b0 = c0 ? atomicAdd(queue_counter(a, t, i0), c0) : 0u;
-    const uint32_t b1 = c1 ? atomicAdd(queue_counter(a, t, i1), c1) : 0u;
-    const uint32_t b2 = c2 ? atomicAdd(queue_counter(a, t, i2), c2) : 0u;
+    const uint32_t b0 = c0 ? atomicAdd(queue_counter(t, i0), c0) : 0u;
+    const uint32_t b1 = c1 ? atomicAdd(queue_counter(t, i1), c1) : 0u;
+    const uint32_t b2 = c2 ? atomicAdd(queue_counter(t, i2), c2) : 0u;
     const uint32_t n = a.g.n;
 #pragma unroll
     for (int j = 0; j < U; ++j) {
@@ -284,11 +284,12 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
         } else if (kind[j] == 2u) {
             r[j] = atomicMin(a.ws.tag + v[j], nb[j]);
         } else if (kind[j] == 3u) {
-            atomicMin(&a.ws.ctl->pend_min[t.pend_sel].v, nb[j]);
+            atomicMin(t.c.at(kCPmin + t.pend_sel), nb[j]);
             r[j] = atomicMin(a.ws.tag + v[j], kTagPending);
-            // the pending minimum steers the next decision; a phase run by
-            // one CTA reaches that decision through __syncthreads alone,
-            // which does not wait for a reduction whose result is unused
+            // the pending minimum and tag steer the next decision and the
+            // next re-bucketing, which a phase run by one CTA reaches through
+            // __syncthreads alone: it does not wait for a global reduction
+            // whose result is unused (a shared-memory minimum it does order)
             __threadfence();
         }
     }

@@ -47,6 +47,19 @@ __device__ __forceinline__ Exec cta_exec() {
     return x;
 }
 
+// The list counters in global memory, and the global home of word i of the
+// deciding CTA's shared copy (counters, then the statistics words).
+__device__ __forceinline__ Ctrs global_ctrs(Ctl *ctl) { return Ctrs{&ctl->ring_cnt[0].v, 32u}; }
+__device__ __forceinline__ uint32_t *counter_home(Ctl *ctl, uint32_t i) {
+    switch (i) {
+        case kSPhases: return &ctl->st_phases;
+        case kSBuckets: return &ctl->st_buckets;
+        case kSPending: return &ctl->st_pending_scans;
+        case kSSolo: return &ctl->st_solo_phases;
+        default: return global_ctrs(ctl).at(i);
+    }
+}
+
 // The decision of a barrier as published (Ctl::pubw): kPubWords fields, each
 // in the low half of a 64-bit word whose high half is the barrier generation.
 enum PubField : uint32_t { kPubState = 0, kPubB, kPubW, kPubEpoch, kPubHround, kPubInst, kPubItems, kPubWords };
@@ -135,7 +148,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
         const uint32_t total = __shfl_sync(FULL, incl, 31);
         if (total) {
             uint32_t dbase = 0;
-            if (lane == 31) dbase = atomicAdd(&ctl->desc_cnt.v, total);
+            if (lane == 31) dbase = atomicAdd(t.c.at(kCDesc), total);
             dbase = __shfl_sync(FULL, dbase, 31);
             if (dbase + total <= a.ws.desc_cap) {
                 // float64 distances do not fit the descriptor: the relaxation
@@ -160,7 +173,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             const uint32_t htotal = __shfl_sync(FULL, hincl, 31);
             if (htotal) {
                 uint32_t hbase = 0;
-                if (lane == 31) hbase = atomicAdd(&ctl->hdesc_cnt.v, htotal);
+                if (lane == 31) hbase = atomicAdd(t.c.at(kCHdesc), htotal);
                 hbase = __shfl_sync(FULL, hbase, 31);
                 if (hbase + htotal <= a.ws.desc_cap) {
                     write_descs(a.ws.hdesc, hbase, htotal, hincl - hn, u, 0u, e, he);
@@ -173,7 +186,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
     cand_drain<WT>(a, t, nc, imp);
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
-    if (lane == 0 && my_edges) atomicAdd(&ctl->edge_cnt.v, my_edges);
+    if (lane == 0 && my_edges) atomicAdd(t.c.at(kCEdge), my_edges);
 }
 
 // Warp-collective: relaxes one chunk [first, end) (<= kDescEdges edges) of
@@ -245,7 +258,7 @@ __device__ void relax_heavy(const SsspArgs &a, const Targets &t, const Exec &x, 
     }
     cand_drain<WT>(a, t, nc, imp);
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
-    if (lane == 0 && my_edges) atomicAdd(&a.ws.ctl->edge_cnt.v, my_edges);
+    if (lane == 0 && my_edges) atomicAdd(t.c.at(kCEdge), my_edges);
 }
 
 // ------------------------------------------------------------------ EDGES
@@ -270,9 +283,8 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exe
 // ring; the rest go to the other pending list.
 template <int WT>
 __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
-                                 uint32_t count) {
+                                 uint32_t count, const Ctrs &c) {
     const uint32_t n = a.g.n;
-    Ctl *ctl = a.ws.ctl;
     const uint32_t *list = a.ws.pend + (size_t)U.pend_sel * n;
     Targets t;
     t.cur_hi = 0;
@@ -281,6 +293,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     t.fq_next = 0;
     t.pend_sel = U.pend_sel ^ 1u;
     t.scr = scr;
+    t.c = c;
     uint32_t stale = 0;
     for (uint32_t base = x.tid - lane_id(); base < count; base += x.nthreads) {
         const uint32_t i = base + lane_id();
@@ -296,7 +309,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
                     a.ws.tag[v[0]] = nb;
                     q[0] = 1 + (int)(nb % kNB);
                 } else {
-                    atomicMin(&ctl->pend_min[t.pend_sel].v, nb);
+                    atomicMin(c.at(kCPmin + t.pend_sel), nb);
                     q[0] = kNB + 1;
                 }
             }
@@ -310,7 +323,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     __threadfence();
     // entries that had already left the pending list (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) stale += __shfl_down_sync(0xffffffffu, stale, o);
-    if (lane_id() == 0 && stale) atomicAdd(&ctl->edge_cnt.v, stale);
+    if (lane_id() == 0 && stale) atomicAdd(c.at(kCEdge), stale);
 }
 
 // ------------------------------------------------------ batched instances
@@ -368,8 +381,7 @@ __device__ void finish_instance(const SsspArgs &a, const Exec &x, uint32_t &imp)
 // Runs the phase U.phase with executor x (grid or one CTA).
 template <int WT>
 __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, WarpScratch *scr,
-                          uint32_t &imp) {
-    Ctl *ctl = a.ws.ctl;
+                          uint32_t &imp, const Ctrs &c) {
     const uint32_t n = a.g.n;
     Targets t;
     t.cur_hi = U.b + U.span;   // the bucket covers base buckets [b, b + span)
@@ -378,6 +390,7 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     t.fq_next = (U.epoch + 1) % 3u;
     t.pend_sel = U.pend_sel;
     t.scr = scr;
+    t.c = c;
     const bool full = U.full != 0;
     // the input size comes with the decision (U.items); the counters are
     // read only where it was not published
@@ -388,24 +401,24 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
             // the other (independent: no barrier between them)
             for (uint32_t j = 0; j < U.span; ++j) {
                 const uint32_t bk = U.b + j;
-                const uint32_t c = (pub && U.span == 1u) ? U.items : __ldcg(&ctl->ring_cnt[bk % kNB].v);
-                scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n, min(c, n), bk, full, U.hround,
+                const uint32_t cnt = (pub && U.span == 1u) ? U.items : ld_relaxed_any(c.at(kCRing + bk % kNB));
+                scan_frontier<WT>(a, t, x, a.ws.ring + (size_t)(bk % kNB) * n, min(cnt, n), bk, full, U.hround,
                                   imp);
             }
             break;
         case kPhLight:
             scan_frontier<WT>(a, t, x, a.ws.fq + (size_t)(U.epoch % 3u) * n,
-                              min(pub ? U.items : __ldcg(&ctl->fq_cnt[U.epoch % 3u].v), n), kTagInit, full,
+                              min(pub ? U.items : ld_relaxed_any(c.at(kCFq + U.epoch % 3u)), n), kTagInit, full,
                               U.hround, imp);
             break;
         case kPhHeavy:
-            relax_heavy<WT>(a, t, x, min(pub ? U.items : __ldcg(&ctl->hdesc_cnt.v), a.ws.desc_cap), imp);
+            relax_heavy<WT>(a, t, x, min(pub ? U.items : ld_relaxed_any(c.at(kCHdesc)), a.ws.desc_cap), imp);
             break;
         case kPhEdges:
-            relax_descriptors<WT>(a, t, x, min(pub ? U.items : __ldcg(&ctl->desc_cnt.v), a.ws.desc_cap), imp);
+            relax_descriptors<WT>(a, t, x, min(pub ? U.items : ld_relaxed_any(c.at(kCDesc)), a.ws.desc_cap), imp);
             break;
         case kPhPending:
-            rebucket_pending<WT>(a, U, x, scr, min(pub ? U.items : __ldcg(&ctl->pend_cnt[U.pend_sel].v), n));
+            rebucket_pending<WT>(a, U, x, scr, min(pub ? U.items : ld_relaxed_any(c.at(kCPend + U.pend_sel)), n), c);
             break;
         case kPhInit:
             init_instance(a, U, x);
@@ -473,7 +486,7 @@ __device__ __forceinline__ void mlp_eval(const float *__restrict__ P, const floa
 // fixed schedule keeps span_fixed base widths; the learned one evaluates the
 // controller on the occupancy of the next base buckets, the run so far and
 // the graph.  GBS_F_FEATURES records the controller input.
-__device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint32_t nb, uint32_t lim,
+__device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, const uint32_t *sc, uint32_t nb, uint32_t lim,
                                               uint32_t ring_lo, uint32_t ring_hi, uint32_t pend, uint32_t pm,
                                               uint32_t &span_out, uint32_t &full_out, uint32_t &first_items) {
     const unsigned FULL = 0xffffffffu;
@@ -504,7 +517,7 @@ __device__ __forceinline__ void decide_bucket(const SsspArgs &a, Ctl *ctl, uint3
         auto first = [&](uint32_t k) {   // entries of base buckets [nb, nb + k), k <= 32
             return (float)__shfl_sync(FULL, incl, k - 1u);
         };
-        const uint32_t st_b = ld_relaxed(&ctl->st_buckets), st_p = ld_relaxed(&ctl->st_phases);
+        const uint32_t st_b = sc[kSBuckets], st_p = sc[kSPhases];
         float f[kFeat];
         f[0] = __log2f(1.f + first(1));
         f[1] = __log2f(1.f + first(2));
@@ -584,21 +597,22 @@ __device__ __forceinline__ Uniform advance_uniform(const Uniform &U, uint32_t ne
 // instance from the queue (INIT) or stops.
 template <bool Batch>
 __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool was_solo, bool &solo,
-                                    uint32_t *s_pub) {
+                                    uint32_t *s_pub, uint32_t *sc) {
     Ctl *ctl = a.ws.ctl;
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
-    // one round trip: every counter the decision needs is loaded at once
-    const uint32_t ring_lo = ld_relaxed(&ctl->ring_cnt[lane].v);
-    const uint32_t ring_hi = ld_relaxed(&ctl->ring_cnt[lane + 32].v);
-    const uint32_t desc_cnt = ld_relaxed(&ctl->desc_cnt.v);
-    const uint32_t edge_cnt = ld_relaxed(&ctl->edge_cnt.v);
-    const uint32_t fq_next = ld_relaxed(&ctl->fq_cnt[(U.epoch + 1u) % 3u].v);
-    const uint32_t fq_cur = ld_relaxed(&ctl->fq_cnt[U.epoch % 3u].v);
-    const uint32_t hd_cnt = ld_relaxed(&ctl->hdesc_cnt.v);
-    const uint32_t pc0 = ld_relaxed(&ctl->pend_cnt[0].v), pc1 = ld_relaxed(&ctl->pend_cnt[1].v);
-    const uint32_t pm0 = ld_relaxed(&ctl->pend_min[0].v), pm1 = ld_relaxed(&ctl->pend_min[1].v);
+    // the error word is the one global read; it is first used at the end
     const uint32_t err = ld_relaxed(&ctl->error);
+    const uint32_t ring_lo = sc[kCRing + lane];
+    const uint32_t ring_hi = sc[kCRing + lane + 32];
+    const uint32_t desc_cnt = sc[kCDesc];
+    const uint32_t edge_cnt = sc[kCEdge];
+    const uint32_t fq_next = sc[kCFq + (U.epoch + 1u) % 3u];
+    const uint32_t fq_cur = sc[kCFq + U.epoch % 3u];
+    const uint32_t hd_cnt = sc[kCHdesc];
+    const uint32_t pc0 = sc[kCPend], pc1 = sc[kCPend + 1];
+    const uint32_t pm0 = sc[kCPmin], pm1 = sc[kCPmin + 1];
+    __syncwarp();   // every lane has read the counters before lane 0 resets them
     auto ring_count = [&](uint32_t bucket) {
         const uint32_t slot = bucket % kNB;
         const uint32_t lo = __shfl_sync(FULL, ring_lo, slot & 31u);
@@ -686,7 +700,6 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         next = kPhDone;
         if (lane == 0) atomicCAS(&ctl->error, 0u, (uint32_t)kErrGuard);
     }
-    if (err) next = kPhDone;
     Uniform N = advance_uniform(U, next, nb);
     if (take) {
         N.inst = inst;
@@ -701,7 +714,7 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     uint32_t first_items = 0;   // LIGHT_FIRST: entries of every list the new bucket spans
     if (next == kPhLightFirst) {
         uint32_t span, full;
-        decide_bucket(a, ctl, nb, U.W + kNB, ring_lo, ring_hi, ps2 ? pc1 : pc0, ps2 ? pm1 : pm0, span, full,
+        decide_bucket(a, ctl, sc, nb, U.W + kNB, ring_lo, ring_hi, ps2 ? pc1 : pc0, ps2 ? pm1 : pm0, span, full,
                       first_items);
         N.span = span;
         N.full = full;
@@ -720,6 +733,14 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
     // small re-bucketing of the pending list runs on this CTA like any small
     // scan
     solo = next < kPhDone && (next == kPhEdges ? items <= a.solo_desc : items <= a.solo_items);
+    // an error raised anywhere ends the run (the counter resets below are
+    // then moot); applied last so the global read overlaps the decision
+    if (err) {
+        next = kPhDone;
+        N.phase = kPhDone;
+        solo = false;
+    }
+    __syncwarp();   // the controller inputs read from sc come before the updates
     if (lane == 0) {
         if ((a.flags & GBS_F_TRACE) && a.ws.trace) {
             const uint32_t ti = ctl->trace_n;
@@ -749,10 +770,10 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             r.done = (U.phase == kPhFinish && !err) ? 1u : 0u;
             r.error = err;
             r.group = a.group;
-            r.phases = ctl->st_phases;
-            r.buckets = ctl->st_buckets;
-            r.pending_scans = ctl->st_pending_scans;
-            r.solo_phases = ctl->st_solo_phases;
+            r.phases = sc[kSPhases];
+            r.buckets = sc[kSBuckets];
+            r.pending_scans = sc[kSPending];
+            r.solo_phases = sc[kSSolo];
             r.pad = 0;
             r.reached = __ldcg(&ctl->st_reached);
             r.edges_reached = __ldcg(&ctl->st_edges_reached);
@@ -761,22 +782,22 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
             r.end_ns = globaltimer();
             a.res[U.inst] = r;
         }
-        if (U.phase < kPhDone) ctl->st_phases += 1;
-        if (U.phase == kPhLightFirst) ctl->st_buckets += 1;
+        if (U.phase < kPhDone) sc[kSPhases] += 1;
+        if (U.phase == kPhLightFirst) sc[kSBuckets] += 1;
         if (U.phase == kPhPending) {
-            ctl->st_pending_scans += 1;
-            ctl->pend_cnt[U.pend_sel].v = 0;          // the list just re-bucketed
-            ctl->pend_min[U.pend_sel].v = kTagInit;
+            sc[kSPending] += 1;
+            sc[kCPend + U.pend_sel] = 0;          // the list just re-bucketed
+            sc[kCPmin + U.pend_sel] = kTagInit;
         }
-        if (was_solo) ctl->st_solo_phases += 1;
-        if (next == kPhPending) ctl->edge_cnt.v = 0;   // counts stale entries there
+        if (was_solo) sc[kSSolo] += 1;
+        if (next == kPhPending) sc[kCEdge] = 0;   // counts stale entries there
         if (next == kPhLight || next == kPhHeavy || next == kPhLightFirst) {
-            ctl->fq_cnt[(N.epoch + 1u) % 3u].v = 0;
-            ctl->desc_cnt.v = 0;
-            ctl->edge_cnt.v = 0;
+            sc[kCFq + (N.epoch + 1u) % 3u] = 0;
+            sc[kCDesc] = 0;
+            sc[kCEdge] = 0;
             // heavy descriptors of the next heavy round start over once the
             // last round's are relaxed, and at every new bucket
-            if (U.phase == kPhHeavy || next == kPhLightFirst) ctl->hdesc_cnt.v = 0;
+            if (U.phase == kPhHeavy || next == kPhLightFirst) sc[kCHdesc] = 0;
         }
         // the decision, in the layout the release publishes
         s_pub[kPubState] = pack_state(N);
@@ -788,30 +809,30 @@ __device__ inline void control_step(const SsspArgs &a, const Uniform &U, bool wa
         s_pub[kPubItems] = next < kPhDone ? items : kNoItems;
     }
     if (bucket_end) {   // the lists of the finished bucket
-        if (lane < U.span) ctl->ring_cnt[(U.b + lane) % kNB].v = 0u;
-        if (lane + 32u < U.span) ctl->ring_cnt[(U.b + 32u + lane) % kNB].v = 0u;
+        if (lane < U.span) sc[kCRing + (U.b + lane) % kNB] = 0u;
+        if (lane + 32u < U.span) sc[kCRing + (U.b + 32u + lane) % kNB] = 0u;
     }
     if (take && next == kPhInit) {
         // every list of the new instance starts empty; the source waits in
         // ring bucket 0 (list slot 0, entry 0)
-        ctl->ring_cnt[lane].v = 0u;
-        ctl->ring_cnt[lane + 32].v = 0u;
+        sc[kCRing + lane] = 0u;
+        sc[kCRing + lane + 32] = 0u;
         __syncwarp();
         if (lane == 0) {
-            ctl->ring_cnt[0].v = 1u;
+            sc[kCRing] = 1u;
             a.ws.ring[0] = a.inst[inst].source;
-            for (int i = 0; i < 3; ++i) ctl->fq_cnt[i].v = 0u;
+            for (int i = 0; i < 3; ++i) sc[kCFq + i] = 0u;
+            sc[kCHdesc] = 0u;
             for (int i = 0; i < 2; ++i) {
-                ctl->hdesc_cnt.v = 0u;
-                ctl->pend_cnt[i].v = 0u;
-                ctl->pend_min[i].v = kTagInit;
+                sc[kCPend + i] = 0u;
+                sc[kCPmin + i] = kTagInit;
             }
-            ctl->desc_cnt.v = 0u;
-            ctl->edge_cnt.v = 0u;
-            ctl->st_buckets = 0u;
-            ctl->st_phases = 0u;
-            ctl->st_pending_scans = 0u;
-            ctl->st_solo_phases = 0u;
+            sc[kCDesc] = 0u;
+            sc[kCEdge] = 0u;
+            sc[kSBuckets] = 0u;
+            sc[kSPhases] = 0u;
+            sc[kSPending] = 0u;
+            sc[kSSolo] = 0u;
             ctl->st_improvements = 0ull;
             ctl->st_reached = 0ull;
             ctl->st_edges_reached = 0ull;
@@ -853,6 +874,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
     const unsigned FULL = 0xffffffffu;
     __shared__ uint32_t s_flag[2];
     __shared__ uint32_t s_pub[kPubWords];
+    __shared__ uint32_t s_cnt[kCtrShared];   // the deciding CTA's copy of the list counters
     __syncthreads();
     if (threadIdx.x == 0) {
         // GBS_F_TEST_STALL: CTA 0 skips its first arrival (failure-path test)
@@ -866,17 +888,34 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
     if (s_flag[0]) {
         const unsigned long long ts = globaltimer();
         bool was_solo = false;
+        // the counters, at rest, into shared memory (one round trip): every
+        // decision of this barrier and every phase this CTA runs alone reads
+        // and updates the copy, which goes back before the release
+        if (threadIdx.x < 32) {
+            uint32_t v[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t i = lane_id() + 32u * k;
+                v[k] = i < (uint32_t)kCtrShared ? ld_relaxed(counter_home(ctl, i)) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t i = lane_id() + 32u * k;
+                if (i < (uint32_t)kCtrShared) s_cnt[i] = v[k];
+            }
+            __syncwarp();
+        }
         for (;;) {
             if (threadIdx.x < 32) {
                 bool solo = false;
-                control_step<Batch>(a, U, was_solo, solo, s_pub);
+                control_step<Batch>(a, U, was_solo, solo, s_pub, s_cnt);
                 if (threadIdx.x == 0) s_flag[1] = solo && (globaltimer() - ts) < a.wait_ns / 4;
             }
             __syncthreads();
             adopt_published(s_pub, U);
-            const bool solo = s_flag[1] != 0;
-            __syncthreads();
-            if (!solo) break;
+            // s_pub and s_flag are written again only after the phase's
+            // __syncthreads below
+            if (s_flag[1] == 0) break;
             // A re-bucketing of the pending list on this CTA is fenced by
             // every thread on both sides: the phases before it wrote the
             // entries, tags and distances it reads, and the decision after it
@@ -890,7 +929,7 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
                 __threadfence();
                 __syncthreads();
             }
-            run_phase<WT>(a, U, cta_exec(), scr, imp);
+            run_phase<WT>(a, U, cta_exec(), scr, imp, Ctrs{s_cnt, 1u});
             if (U.phase == kPhPending) __threadfence();
             // the decision is taken by this CTA: __syncthreads makes every
             // global access of the phase (the fire-and-forget tag and pend_min
@@ -900,10 +939,19 @@ __device__ __forceinline__ void barrier_and_decide(const SsspArgs &a, Uniform &U
             __syncthreads();
             was_solo = true;
         }
-        // one release store per word; lane 0's also releases the counter reset
-        if (threadIdx.x < kPubWords) {
-            if (threadIdx.x == 0) ctl->bar_count = 0;
-            st_release64(&ctl->pubw[threadIdx.x], tag | s_pub[threadIdx.x]);
+        // the counters back to global memory, then one release store per
+        // published word; lane 0's also releases the barrier counter reset
+        if (threadIdx.x < 32) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t i = lane_id() + 32u * k;
+                if (i < (uint32_t)kCtrShared) *counter_home(ctl, i) = s_cnt[i];
+            }
+            __syncwarp();
+            if (threadIdx.x < kPubWords) {
+                if (threadIdx.x == 0) ctl->bar_count = 0;
+                st_release64(&ctl->pubw[threadIdx.x], tag | s_pub[threadIdx.x]);
+            }
         }
     } else {
         if (threadIdx.x < 32) {
@@ -965,7 +1013,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_persistent(SsspArgs a) {
     U.t0 = globaltimer();
     uint32_t imp = 0;
     while (U.phase != kPhDone) {
-        run_phase<WT>(a, U, group_exec(a), scr, imp);
+        run_phase<WT>(a, U, group_exec(a), scr, imp, global_ctrs(ctl));
         barrier_and_decide<WT, false>(a, U, scr, imp);
     }
     for (int o = 16; o > 0; o >>= 1) imp += __shfl_down_sync(0xffffffffu, imp, o);
@@ -1026,7 +1074,7 @@ __global__ void __launch_bounds__(kTPB, 1) sssp_batch(SsspArgs base, const Works
             loaded = U.inst;
             U.t0 = globaltimer();   // the run-time limit applies per instance
         }
-        run_phase<WT>(s_a, U, group_exec(s_a), scr, imp);
+        run_phase<WT>(s_a, U, group_exec(s_a), scr, imp, global_ctrs(ctl));
         barrier_and_decide<WT, true>(s_a, U, scr, imp);
     }
     if (group_rank(s_a) == 0 && threadIdx.x == 0) {
