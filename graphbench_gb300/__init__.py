@@ -62,7 +62,8 @@ class Params(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("light", ctypes.c_double),
                 ("flags", ctypes.c_uint32), ("wait_limit_ms", ctypes.c_uint32),
                 ("solo_entries", ctypes.c_uint32), ("solo_descs", ctypes.c_uint32),
-                ("inline_edges", ctypes.c_uint32), ("full_items", ctypes.c_uint32)]
+                ("inline_edges", ctypes.c_uint32), ("full_items", ctypes.c_uint32),
+                ("fuse_rounds", ctypes.c_uint32)]
 
 
 class PhaseRec(ctypes.Structure):
@@ -76,6 +77,7 @@ PHASE_KINDS = {0: "scan_bucket", 1: "scan_light", 2: "heavy", 3: "relax", 4: "pe
 F_TRACE = 0x2
 F_NO_SOLO = 0x4
 F_BC_SINGLE = 0x20
+F_NO_FUSE = 0x40
 F_FEATURES = 0x8
 F_LEARNED = 0x10
 N_FEAT = 16
@@ -139,7 +141,8 @@ class BatchParams(ctypes.Structure):
     _fields_ = [("delta", ctypes.c_double), ("delta_scale", ctypes.c_double), ("light", ctypes.c_double),
                 ("group_ctas", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("wait_limit_ms", ctypes.c_uint32), ("solo_entries", ctypes.c_uint32),
-                ("solo_descs", ctypes.c_uint32), ("inline_edges", ctypes.c_uint32)]
+                ("solo_descs", ctypes.c_uint32), ("inline_edges", ctypes.c_uint32),
+                ("fuse_rounds", ctypes.c_uint32)]
 
 
 class InstStats(ctypes.Structure):
@@ -456,7 +459,7 @@ class Graph:
     @staticmethod
     def params(delta: float | None = None, light: float | None = None, flags: int = 0,
                wait_limit_ms: int = 0, solo_entries: int = 0, solo_descs: int = 0,
-               inline_edges: int = 0, full_items: int = 0) -> Params:
+               inline_edges: int = 0, full_items: int = 0, fuse_rounds: int = 0) -> Params:
         p = Params()
         p.delta = float(delta) if delta else 0.0
         p.light = float(light) if light is not None else -1.0
@@ -466,6 +469,7 @@ class Graph:
         p.solo_descs = solo_descs
         p.inline_edges = inline_edges
         p.full_items = full_items
+        p.fuse_rounds = fuse_rounds
         return p
 
     def trace(self) -> list[dict]:
@@ -531,7 +535,7 @@ class Graph:
         _check(lib.gbs_autotune(self._h, _ptr(src), len(src), float(budget_ms), ctypes.byref(rep)), "gbs_autotune")
         b = rep.best
         kw = {"delta": b.delta, "light": b.light, "solo_entries": b.solo_entries, "solo_descs": b.solo_descs,
-              "inline_edges": b.inline_edges}
+              "inline_edges": b.inline_edges, "fuse_rounds": b.fuse_rounds}
         r = {k: getattr(rep, k) for k, _ in TuneReport._fields_ if k != "best"}
         r["best"] = dict(kw)
         return kw, r
@@ -740,7 +744,7 @@ def run_sspath_arr(gs: TCsr, source: int, delta: float) -> np.ndarray:
 # --------------------------------------------------------------- batched
 def batch_params(delta: float | None = None, delta_scale: float | None = None, light: float | None = None,
                  group_ctas: int = 0, flags: int = 0, wait_limit_ms: int = 0, solo_entries: int = 0,
-                 solo_descs: int = 0, inline_edges: int = 0) -> BatchParams:
+                 solo_descs: int = 0, inline_edges: int = 0, fuse_rounds: int = 0) -> BatchParams:
     """light=None: light bound = delta; light=math.inf: no light/heavy split."""
     p = BatchParams()
     p.delta = float(delta) if delta else 0.0
@@ -752,6 +756,7 @@ def batch_params(delta: float | None = None, delta_scale: float | None = None, l
     p.solo_entries = solo_entries
     p.solo_descs = solo_descs
     p.inline_edges = inline_edges
+    p.fuse_rounds = fuse_rounds
     return p
 
 

@@ -191,7 +191,8 @@ gbs_status build_plan(gbs_plan *p, const gbs_batch_params *bp, int sms, uint32_t
     p->host_res.resize(p->count);
 
     SsspArgs a{};
-    a.flags = bp ? (bp->flags & (GBS_F_NO_SOLO | GBS_F_TEST_STALL)) : 0u;
+    a.flags = bp ? (bp->flags & (GBS_F_NO_SOLO | GBS_F_NO_FUSE | GBS_F_TEST_STALL)) : 0u;
+    a.fuse_rounds = (a.flags & GBS_F_NO_FUSE) ? 0u : ((bp && bp->fuse_rounds) ? bp->fuse_rounds : kFuseRounds);
     const bool no_solo = (a.flags & GBS_F_NO_SOLO) != 0;
     a.solo_items = no_solo ? 0u : ((bp && bp->solo_entries) ? bp->solo_entries : 1024u);
     a.solo_desc = no_solo ? 0u : ((bp && bp->solo_descs) ? bp->solo_descs : 64u);

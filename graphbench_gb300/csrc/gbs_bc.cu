@@ -1056,7 +1056,7 @@ gbs_status run_bc(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_p
         gbs_batch_params bp{};
         bp.delta = p.delta;
         bp.light = p.light;
-        bp.flags = p.flags & GBS_F_NO_SOLO;
+        bp.flags = p.flags & (GBS_F_NO_SOLO | GBS_F_NO_FUSE);
         bp.wait_limit_ms = p.wait_limit_ms;
         bp.solo_entries = p.solo_entries;
         bp.solo_descs = p.solo_descs;

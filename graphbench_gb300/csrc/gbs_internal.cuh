@@ -38,6 +38,10 @@ constexpr uint32_t kTagPending = 0xFFFFFFFEu;
 constexpr uint32_t kBucketMax = 0xFFFFFF00u;
 constexpr unsigned long long kUnreached = ~0ull;
 constexpr int kTPB = 1024;              // threads per CTA of the persistent kernel
+// Default bucket fusion rounds per warp and scan.  Plain width, 4096^2 grid
+// (kernel ms): 1 231, 2 224, 4 240, 8 242; at 64 plain widths 1 96, 2 89,
+// 4 83, 8 80 (the autotuner picks per graph); R-MAT 20 / 22 flat.
+constexpr uint32_t kFuseRounds = 2;
 
 enum ErrCode : uint32_t {
     kErrNone = 0,
@@ -236,6 +240,7 @@ struct SsspArgs {
     uint32_t inline_max;    // rows up to this long are relaxed by the scanning warp
     uint32_t full_items;    // kCtrlFixed: a bucket whose lists hold at most this many entries when it
                             // starts relaxes whole rows (no heavy phase)
+    uint32_t fuse_rounds;   // bucket fusion rounds per warp in whole-row scans (0: none)
     // bucket-width controller
     uint32_t ctrl;          // CtrlMode
     uint32_t span_fixed;    // kCtrlFixed: base widths per bucket (0 or 1 = plain delta-stepping)
@@ -305,6 +310,10 @@ __device__ __forceinline__ uint2 ld_stream(const uint2 *p) {
     return v;
 }
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+// Fire-and-forget line fetches: into this SM's L1 (a row this warp reads
+// soon) or into L2 (a row another SM reads in a later phase).
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // Sets the message gbs_last_error returns on the calling thread.
 void set_last_error(const char *msg);

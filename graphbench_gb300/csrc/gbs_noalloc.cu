@@ -249,6 +249,7 @@ extern "C" gbs_status gbs_sssp_noalloc(uint32_t n, uint64_t m, const uint32_t *r
     a.no_heavy = 1;  // every edge is light (see mid above)
     a.inline_max = kInlineEdges;
     a.full_items = kFullItems;
+    a.fuse_rounds = kFuseRounds;
     a.ctrl = kCtrlFixed;
     a.span_fixed = 1;
     a.wait_ns = 4000ull * 1000000ull;

@@ -152,6 +152,24 @@ struct Targets {
     uint32_t pend_sel;    // pending list to append to
     WarpScratch *scr;     // this warp's shared-memory scratch
     Ctrs c;               // the list counters (global, or the deciding CTA's shared copy)
+    uint32_t fuse;        // 1: bucket fusion (Local) in this phase
+};
+
+// Bucket fusion.  During a scan that relaxes whole rows, a target that
+// improves into the current bucket is kept by the lane whose atomicMin
+// improved it (one slot per lane) and relaxed by that warp later in the same
+// phase, instead of joining the next frontier and costing a phase of its
+// own: chains of light hops inside a bucket (high-diameter graphs) run
+// without a barrier per hop.  A kept target is relaxed with the distance its
+// own improvement wrote, so each improvement is relaxed at least once
+// (possibly twice, if the frontier holds the vertex as well) and the least
+// fixpoint is the same; a lane whose slot is taken sends the target to the
+// next frontier as before.
+constexpr uint32_t kNoLocal = 0xFFFFFFFFu;   // empty slot
+constexpr uint32_t kNoKeep = 0xFFFFFFFEu;    // closed slot: the warp's last fusion round
+struct Local {
+    uint32_t v;   // the kept vertex, or kNoLocal / kNoKeep
+    uint32_t d;   // distance bits written by the improvement
 };
 
 // Queue ids: -1 none, 0 next frontier, 1..kNB ring slots, kNB+1 pending.
@@ -260,7 +278,8 @@ __device__ __forceinline__ bool edge_sum(typename Arith<WT>::D du, typename Arit
 template <int WT, int U>
 __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &t, const bool (&cand)[U],
                                               const uint32_t (&v)[U], const uint32_t (&uo)[U],
-                                              const typename Arith<WT>::D (&nd)[U], int (&q)[U], uint32_t &imp) {
+                                              const typename Arith<WT>::D (&nd)[U], int (&q)[U], uint32_t &imp,
+                                              Local &loc) {
     unsigned long long old[U];
 #pragma unroll
     for (int j = 0; j < U; ++j) old[j] = cand[j] ? atomicMin(a.ws.dp + v[j], pack_dist<WT>(nd[j], uo[j])) : 0ull;
@@ -280,7 +299,20 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
         r[j] = 0;
         if (kind[j] == 1u) {
             atomicMin(a.ws.tag + v[j], nb[j]);
-            r[j] = atomicExch(a.ws.fst + v[j], t.stamp_next);
+            bool kept = false;
+            if constexpr (WT != kWF64) {
+                if (t.fuse && loc.v == kNoLocal) {
+                    loc.v = v[j];
+                    loc.d = nd[j];
+                    kept = true;
+                }
+            }
+            if (kept) {
+                kind[j] = 4u;   // relaxed by this warp later in the phase
+                prefetch_l1(a.g.row + v[j]);
+            } else {
+                r[j] = atomicExch(a.ws.fst + v[j], t.stamp_next);
+            }
         } else if (kind[j] == 2u) {
             r[j] = atomicMin(a.ws.tag + v[j], nb[j]);
         } else if (kind[j] == 3u) {
@@ -296,7 +328,10 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
 #pragma unroll
     for (int j = 0; j < U; ++j) {
         q[j] = -1;
-        if (kind[j] == 1u && r[j] != t.stamp_next) q[j] = 0;
+        if (kind[j] == 1u && r[j] != t.stamp_next) {
+            q[j] = 0;
+            prefetch_l2(a.g.row + v[j]);   // the next frontier scan reads it
+        }
         else if (kind[j] == 2u && r[j] > nb[j]) q[j] = 1 + (int)(nb[j] % kNB);
         else if (kind[j] == 3u && r[j] == kTagInit) q[j] = kNB + 1;
     }
@@ -307,7 +342,7 @@ __device__ __forceinline__ void improve_batch(const SsspArgs &a, const Targets &
 // dependent atomics (distance, tag, list) per U x 32 candidates.
 template <int WT, int U>
 __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t take,
-                                           uint32_t &imp) {
+                                           uint32_t &imp, Local &loc) {
     const unsigned lane = lane_id();
     WarpScratch *s = t.scr;
     uint32_t v1[U], u1[U];
@@ -331,7 +366,7 @@ __device__ __forceinline__ void cand_flush(const SsspArgs &a, const Targets &t, 
     __syncwarp();
     nc -= take;
     int q[U];
-    improve_batch<WT, U>(a, t, c1, v1, u1, n1, q, imp);
+    improve_batch<WT, U>(a, t, c1, v1, u1, n1, q, imp, loc);
     warp_enqueue<U>(a, t, q, v1);
 }
 
@@ -344,7 +379,7 @@ template <int WT, int U>
 __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Targets &t, const bool (&val)[U],
                                                  const uint32_t (&v)[U], const typename Arith<WT>::Wt (&w)[U],
                                                  const uint32_t (&uo)[U], const typename Arith<WT>::D (&duo)[U],
-                                                 uint32_t &nc, uint32_t &imp) {
+                                                 uint32_t &nc, uint32_t &imp, Local &loc) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     unsigned long long cur[U];
@@ -370,16 +405,17 @@ __device__ __forceinline__ void relax_candidates(const SsspArgs &a, const Target
             }
             nc += (uint32_t)__popc(m);
             __syncwarp();
-            if (nc >= (uint32_t)kFlush) cand_flush<WT, kFlush / 32>(a, t, nc, kFlush, imp);
+            if (nc >= (uint32_t)kFlush) cand_flush<WT, kFlush / 32>(a, t, nc, kFlush, imp, loc);
         }
     }
 }
 
 // Drains the warp's candidate buffer (end of a phase's relaxation work).
 template <int WT>
-__device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t &imp) {
-    if (nc > 32u) cand_flush<WT, kFlush / 32>(a, t, nc, nc, imp);
-    else if (nc) cand_flush<WT, 1>(a, t, nc, nc, imp);
+__device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, uint32_t &nc, uint32_t &imp,
+                                           Local &loc) {
+    if (nc > 32u) cand_flush<WT, kFlush / 32>(a, t, nc, nc, imp, loc);
+    else if (nc) cand_flush<WT, 1>(a, t, nc, nc, imp, loc);
 }
 
 // Warp-collective: relaxes edges [s, s+len) of source u (distance bits du)
@@ -387,7 +423,7 @@ __device__ __forceinline__ void cand_drain(const SsspArgs &a, const Targets &t, 
 template <int WT>
 __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t, uint32_t u,
                                             typename Arith<WT>::D du, uint32_t s, uint32_t len, uint32_t &nc,
-                                            uint32_t &imp) {
+                                            uint32_t &imp, Local &loc) {
     const unsigned FULL = 0xffffffffu;
     const unsigned lane = lane_id();
     uint32_t incl = len;
@@ -427,7 +463,7 @@ __device__ __forceinline__ void relax_group(const SsspArgs &a, const Targets &t,
                 w[j] = weight_at<WT>(a, e, ew);
             }
         }
-        relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
+        relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp, loc);
     }
 }
 

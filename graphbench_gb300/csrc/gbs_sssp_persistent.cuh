@@ -100,6 +100,65 @@ __device__ __forceinline__ void write_descs(uint4 *out, uint32_t base, uint32_t 
 }
 
 // ------------------------------------------------------------------- SCAN
+// Warp-collective: every lane's row range [s, e) of source u (distance bits
+// du; an empty range for a lane without one).  Rows longer than inline_max
+// become descriptors, reserved with one atomic per warp; the others are
+// relaxed by this warp now.  Edges handed to EDGES add to my_edges.
+template <int WT>
+__device__ __forceinline__ void scan_rows(const SsspArgs &a, const Targets &t, uint32_t u,
+                                          typename Arith<WT>::D du, uint32_t s, uint32_t e, uint32_t &my_edges,
+                                          uint32_t &nc, uint32_t &imp, Local &loc) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = lane_id();
+    const uint32_t len = e - s;
+    const uint32_t nd = len > a.inline_max ? (len + kDescEdges - 1) / kDescEdges : 0u;
+    uint32_t incl = nd;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if ((int)lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    if (total) {
+        uint32_t dbase = 0;
+        if (lane == 31) dbase = atomicAdd(t.c.at(kCDesc), total);
+        dbase = __shfl_sync(FULL, dbase, 31);
+        if (dbase + total <= a.ws.desc_cap) {
+            // float64 distances do not fit the descriptor: the relaxation
+            // reads dp[u] again (a fresher value is as valid)
+            write_descs(a.ws.desc, dbase, total, incl - nd, u, WT == kWF64 ? 0u : (uint32_t)du, s, e);
+        } else if (lane == 31) {
+            atomicExch(&a.ws.ctl->error, (uint32_t)kErrCapacity);
+        }
+        my_edges += nd ? len : 0u;
+    }
+    relax_group<WT>(a, t, u, du, s, nd ? 0u : len, nc, imp, loc);
+}
+
+// Bucket fusion: the targets the warp's lanes kept, relaxed in rounds of one
+// per lane (whole rows, long ones as descriptors), at most fuse_rounds of
+// them: the last round keeps nothing, so a long chain goes back to the
+// frontier instead of running hop after hop on one warp while the rest of
+// the grid waits (and relaxing vertices whose distances later drop again).
+// Warp-collective; ends with the candidate buffer drained.
+template <int WT>
+__device__ __forceinline__ void fuse_drain(const SsspArgs &a, const Targets &t, uint32_t &my_edges, uint32_t &nc,
+                                           uint32_t &imp, Local &loc) {
+    const unsigned FULL = 0xffffffffu;
+    cand_drain<WT>(a, t, nc, imp, loc);
+    if (!t.fuse) return;
+    for (uint32_t round = 1; __ballot_sync(FULL, loc.v < kNoKeep); ++round) {
+        const bool has = loc.v < kNoKeep;
+        const uint32_t u = has ? loc.v : 0u;
+        const uint32_t s = has ? __ldg(a.g.row + u) : 0u;
+        const uint32_t e = has ? __ldg(a.g.row + u + 1) : 0u;
+        const typename Arith<WT>::D du = loc.d;
+        loc.v = round < a.fuse_rounds ? kNoLocal : kNoKeep;
+        scan_rows<WT>(a, t, u, du, s, e, my_edges, nc, imp, loc);
+        cand_drain<WT>(a, t, nc, imp, loc);
+    }
+}
+
 // One thread per frontier entry.  vtag != kTagInit keeps only entries whose
 // tag equals it (ring lists may hold entries that moved to a lower bucket).
 // The scan relaxes the light prefix [row, mid) of each row, or the whole row
@@ -114,6 +173,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
     Ctl *ctl = a.ws.ctl;
     uint32_t my_edges = 0;
     uint32_t nc = 0;   // candidates buffered by this warp
+    Local loc{kNoLocal, 0u};
     for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
         const uint32_t i = base + lane;
         uint32_t u = 0, s = 0, e = 0, he = 0;
@@ -136,31 +196,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
         // written after the relaxation below so this latency overlaps it
         uint32_t hold = hround;
         if (ok && !full) hold = atomicExch(a.ws.hst + u, hround);
-        const uint32_t len = e - s;
-        // long rows -> descriptors, reserved with one atomic per warp
-        const uint32_t nd = len > a.inline_max ? (len + kDescEdges - 1) / kDescEdges : 0u;
-        uint32_t incl = nd;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, o);
-            if ((int)lane >= o) incl += y;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        if (total) {
-            uint32_t dbase = 0;
-            if (lane == 31) dbase = atomicAdd(t.c.at(kCDesc), total);
-            dbase = __shfl_sync(FULL, dbase, 31);
-            if (dbase + total <= a.ws.desc_cap) {
-                // float64 distances do not fit the descriptor: the relaxation
-                // reads dp[u] again (a fresher value is as valid)
-                write_descs(a.ws.desc, dbase, total, incl - nd, u, WT == kWF64 ? 0u : (uint32_t)du, s, e);
-            } else if (lane == 31) {
-                atomicExch(&ctl->error, (uint32_t)kErrCapacity);
-            }
-            my_edges += nd ? len : 0u;
-        }
-        // short rows: relaxed by this warp now
-        relax_group<WT>(a, t, u, du, s, nd ? 0u : len, nc, imp);
+        scan_rows<WT>(a, t, u, du, s, e, my_edges, nc, imp, loc);
         if (!full) {
             const uint32_t hlen = (ok && hold != hround) ? he - e : 0u;
             const uint32_t hn = (hlen + kDescEdges - 1) / kDescEdges;
@@ -183,7 +219,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
             }
         }
     }
-    cand_drain<WT>(a, t, nc, imp);
+    fuse_drain<WT>(a, t, my_edges, nc, imp, loc);
     // edges handed to EDGES (statistics / trace)
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
     if (lane == 0 && my_edges) atomicAdd(t.c.at(kCEdge), my_edges);
@@ -194,7 +230,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
 template <int WT>
 __device__ __forceinline__ void relax_chunk(const SsspArgs &a, const Targets &t, uint32_t u,
                                             typename Arith<WT>::D du, uint32_t first, uint32_t end, uint32_t &nc,
-                                            uint32_t &imp) {
+                                            uint32_t &imp, Local &loc) {
     const unsigned lane = lane_id();
     uint32_t v[kUnroll], uo[kUnroll];
     typename Arith<WT>::Wt w[kUnroll];
@@ -214,7 +250,7 @@ __device__ __forceinline__ void relax_chunk(const SsspArgs &a, const Targets &t,
             w[j] = weight_at<WT>(a, e, ew);
         }
     }
-    relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp);
+    relax_candidates<WT>(a, t, val, v, w, uo, duo, nc, imp, loc);
 }
 
 // ------------------------------------------------------------------ HEAVY
@@ -231,6 +267,7 @@ __device__ void relax_heavy(const SsspArgs &a, const Targets &t, const Exec &x, 
     const unsigned lane = lane_id();
     uint32_t nc = 0;   // candidates buffered by this warp
     uint32_t my_edges = 0;
+    Local loc{kNoLocal, 0u};   // heavy phases never fuse
     for (unsigned long long j0 = 0; x.warp + (unsigned long long)x.nwarps * j0 < count; j0 += 32u) {
         const unsigned long long i = x.warp + (unsigned long long)x.nwarps * (j0 + lane);
         uint32_t u = 0, s = 0, len = 0;
@@ -252,11 +289,11 @@ __device__ void relax_heavy(const SsspArgs &a, const Targets &t, const Exec &x, 
             const uint32_t ss = __shfl_sync(FULL, s, src);
             const uint32_t sl = __shfl_sync(FULL, len, src);
             const typename Arith<WT>::D sd = __shfl_sync(FULL, du, src);
-            relax_chunk<WT>(a, t, su, sd, ss, ss + sl, nc, imp);
+            relax_chunk<WT>(a, t, su, sd, ss, ss + sl, nc, imp, loc);
         }
-        relax_group<WT>(a, t, u, du, s, lng ? 0u : len, nc, imp);
+        relax_group<WT>(a, t, u, du, s, lng ? 0u : len, nc, imp, loc);
     }
-    cand_drain<WT>(a, t, nc, imp);
+    cand_drain<WT>(a, t, nc, imp, loc);
     for (int o = 16; o > 0; o >>= 1) my_edges += __shfl_down_sync(FULL, my_edges, o);
     if (lane == 0 && my_edges) atomicAdd(t.c.at(kCEdge), my_edges);
 }
@@ -268,15 +305,16 @@ __device__ void relax_descriptors(const SsspArgs &a, const Targets &t, const Exe
                                   uint32_t &imp) {
     const unsigned lane = lane_id();
     uint32_t nc = 0;   // candidates buffered by this warp
+    Local loc{kNoLocal, 0u};   // EDGES phases never fuse: a descriptor they emitted would be lost
     for (uint32_t c = x.warp; c < count; c += x.nwarps) {
         const uint4 d = __ldcg(a.ws.desc + c);
         // float64 distances do not fit the descriptor: read dp[u] again
         typename Arith<WT>::D du;
         if constexpr (WT == kWF64) du = dist_of<WT>(__ldcg(a.ws.dp + d.x));
         else du = d.y;
-        relax_chunk<WT>(a, t, d.x, du, d.z, d.w, nc, imp);
+        relax_chunk<WT>(a, t, d.x, du, d.z, d.w, nc, imp, loc);
     }
-    cand_drain<WT>(a, t, nc, imp);
+    cand_drain<WT>(a, t, nc, imp, loc);
 }
 
 // Moves pending vertices whose bucket entered the window [W, W+kNB) into the
@@ -294,6 +332,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     t.pend_sel = U.pend_sel ^ 1u;
     t.scr = scr;
     t.c = c;
+    t.fuse = 0;
     uint32_t stale = 0;
     for (uint32_t base = x.tid - lane_id(); base < count; base += x.nthreads) {
         const uint32_t i = base + lane_id();
@@ -392,6 +431,9 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     t.scr = scr;
     t.c = c;
     const bool full = U.full != 0;
+    // bucket fusion in whole-row scans (EDGES could not keep the descriptors
+    // a kept long row emits: the next scan resets their list)
+    t.fuse = (a.fuse_rounds && full && WT != kWF64 && (U.phase == kPhLightFirst || U.phase == kPhLight)) ? 1u : 0u;
     // the input size comes with the decision (U.items); the counters are
     // read only where it was not published
     const bool pub = U.items != kNoItems;

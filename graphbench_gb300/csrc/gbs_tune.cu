@@ -23,6 +23,9 @@ const int kMinExp = -3, kMaxExp = 14;
 const uint32_t kInline[] = {8, 16, 64, 128};
 const uint32_t kSoloEntries[] = {256, 4096, 16384};
 const uint32_t kSoloDescs[] = {16, 256, 1024};
+// Bucket fusion rounds besides the default: wide buckets hold longer light
+// chains (4096^2 grid at 64 plain widths: 2 rounds 89 ms, 8 rounds 80 ms).
+const uint32_t kFuse[] = {1, 4, 8, 16};
 
 struct Budget {
     double limit_ms, used_ms = 0.0;
@@ -132,6 +135,30 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
         }
         return GBS_OK;
     };
+    // 2. fusion rounds at the best width, then the widths next to it again
+    //    with the rounds found
+    {
+        const gbs_params before = best;
+        for (uint32_t v : kFuse)
+            if ((s = try_knob([&](gbs_params &p) { p.fuse_rounds = v; })) != GBS_OK) return s;
+        if (best.fuse_rounds != before.fuse_rounds) {
+            const gbs_params at = best;
+            for (double f : {0.5, 2.0}) {
+                if (!b.left()) break;
+                gbs_params p = at;
+                p.delta = at.delta * f;
+                double ms = 0.0;
+                if ((s = time_single(g, src, p, b, out->runs, ms)) != GBS_OK) return s;
+                ++out->candidates;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = p;
+                    best_scale *= f;
+                }
+            }
+        }
+    }
+    // 3. the other knobs
     for (uint32_t v : kInline)
         if ((s = try_knob([&](gbs_params &p) { p.inline_edges = v; })) != GBS_OK) return s;
     for (uint32_t v : kSoloEntries)
@@ -286,10 +313,16 @@ gbs_status tune_plan(Make make, uint32_t max_blocks, double budget_ms, const gbs
             if ((s = consider(p, t)) != GBS_OK) return s;
         }
     }
-    // 4. inline-row limit
+    // 4. inline-row limit and fusion rounds
     for (uint32_t v : kInline) {
         gbs_batch_params p = best;
         p.inline_edges = v;
+        double t;
+        if ((s = consider(p, t)) != GBS_OK) return s;
+    }
+    for (uint32_t v : kFuse) {
+        gbs_batch_params p = best;
+        p.fuse_rounds = v;
         double t;
         if ((s = consider(p, t)) != GBS_OK) return s;
     }
@@ -328,6 +361,7 @@ gbs_status gbs_autotune_plan_sources(gbs_graph *g, const uint32_t *sources, uint
     seed.solo_entries = sr.best.solo_entries;
     seed.solo_descs = sr.best.solo_descs;
     seed.inline_edges = sr.best.inline_edges;
+    seed.fuse_rounds = sr.best.fuse_rounds;
     return tune_plan(make, batch_blocks(g->device), total * 2.0 / 3.0, &seed, out);
 }
 

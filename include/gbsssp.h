@@ -82,6 +82,11 @@ typedef struct gbs_params {
                                 when it starts relaxes whole rows (light and heavy
                                 edges together, no heavy phase); 0 = max(1024,
                                 vertices / 16) */
+    uint32_t fuse_rounds;    /* bucket fusion: a whole-row scan relaxes the vertices
+                                it improves into the current bucket itself, for up
+                                to this many rounds per warp, before the next ones
+                                wait for the next frontier scan; 0 = 2 (uint32 and
+                                float32 weights; GBS_F_NO_FUSE turns it off) */
 } gbs_params;
 
 #define GBS_F_NO_STATS 0x1u  /* skip the reached-vertex/edge reduction */
@@ -92,6 +97,9 @@ typedef struct gbs_params {
                                 (gbs_graph_set_controller) */
 #define GBS_F_BC_SINGLE 0x20u /* gbs_bc: one single-source launch per source instead of
                                 batched launches of up to 64 sources */
+#define GBS_F_NO_FUSE 0x40u  /* no bucket fusion (gbs_params.fuse_rounds): a vertex
+                                improved into the current bucket always waits for
+                                the next frontier scan */
 /* Failure-path test: one CTA never arrives at the first grid barrier, so every
  * other CTA's bounded wait runs out; the call returns GBS_ERR_TIMEOUT after
  * wait_limit_ms and the device stays usable.  Never set in normal use. */
@@ -426,11 +434,12 @@ typedef struct gbs_batch_params {
     uint32_t group_ctas;   /* CTAs per group (0: one group per instance while the
                               groups' distance words, 8 bytes per vertex each,
                               fit in L2; fewer and wider groups beyond) */
-    uint32_t flags;        /* GBS_F_NO_SOLO */
+    uint32_t flags;        /* GBS_F_NO_SOLO, GBS_F_NO_FUSE */
     uint32_t wait_limit_ms;
     uint32_t solo_entries;
     uint32_t solo_descs;
     uint32_t inline_edges;   /* as gbs_params.inline_edges */
+    uint32_t fuse_rounds;    /* as gbs_params.fuse_rounds */
 } gbs_batch_params;
 
 /* Per-instance result record (device times from %globaltimer). */

@@ -99,19 +99,22 @@ def test_hub_rows_split_into_descriptors(gb, orc):
     run_and_check(gb, orc, a.row, a.col, a.w, src, delta=100000)
 
 
-@pytest.mark.parametrize("mode", ["grid_only", "default", "all_solo"])
+@pytest.mark.parametrize("mode", ["grid_only", "default", "all_solo", "all_solo_no_fuse", "no_fuse"])
 def test_solo_phases_same_result(mode, gb, orc):
     """Phases run by one CTA (small inputs) or by the whole grid give the same
-    result; 'all_solo' makes every phase after the first run on one CTA."""
+    result; 'all_solo' makes every phase after the first run on one CTA;
+    the no_fuse modes turn bucket fusion off."""
     kw = {"grid_only": dict(flags=gb.F_NO_SOLO),
           "default": {},
-          "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30)}[mode]
+          "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30),
+          "all_solo_no_fuse": dict(solo_entries=1 << 30, solo_descs=1 << 30, flags=gb.F_NO_FUSE),
+          "no_fuse": dict(flags=gb.F_NO_FUSE)}[mode]
     a = gb.gen_rmat(13, 16, 11)
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
     _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, **kw)
     if mode == "grid_only":
         assert st["solo_phases"] == 0
-    if mode == "all_solo":
+    if mode.startswith("all_solo"):
         assert st["solo_phases"] >= st["phases"] - 2
     g2 = gb.gen_grid(64, 96, 5, "f32")
     _, _, st2 = run_and_check(gb, orc, g2.row, g2.col, g2.w, 0, **kw)
@@ -187,14 +190,15 @@ def test_pending_list_small_delta(gb, orc):
     assert st["pending_scans"] >= 1
 
 
-@pytest.mark.parametrize("mode", ["default", "all_solo"])
+@pytest.mark.parametrize("mode", ["default", "all_solo", "no_fuse"])
 def test_pending_rebucketing_on_one_cta(mode, gb, orc):
     """Widths far below the largest weight push most vertices past the ring
     window; their re-bucketing runs on the deciding CTA when the pending list
     is small.  Every run must give the oracle's distances and predecessors
     (before the re-bucketing fenced its tag stores and the pending minimum,
     half of these runs on one CTA stopped early or skipped vertices)."""
-    kw = {} if mode == "default" else dict(solo_entries=1 << 30, solo_descs=1 << 30)
+    kw = {"default": {}, "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30),
+          "no_fuse": dict(flags=gb.F_NO_FUSE)}[mode]
     cases = [(gb.gen_grid(54, 83, 107, "u32"), [1, 2, 3]), (gb.gen_grid(47, 71, 205, "f32"), [2.0, 20.0]),
              (gb.gen_rmat(12, 16, 302), [1, 4])]
     pend = 0
@@ -204,6 +208,21 @@ def test_pending_rebucketing_on_one_cta(mode, gb, orc):
                 _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, delta=d, **kw)
                 pend += st["pending_scans"]
     assert pend > 20
+
+
+@pytest.mark.parametrize("wtype", ["u32", "f32"])
+def test_bucket_fusion_fewer_phases_same_result(wtype, gb, orc):
+    """Whole-row scans relax the vertices they improve into the current bucket
+    later in the same phase (bucket fusion).  On a grid, whose buckets hold
+    long chains of light hops, that takes fewer phases than waiting for the
+    next frontier scan each hop; with and without it, on one CTA and on the
+    whole grid, the distances and predecessors are the oracle's."""
+    a = gb.gen_grid(80, 120, 9, wtype)
+    for src in (0, 120 * 40 + 57):
+        for base in (0, gb.F_NO_SOLO):
+            _, _, on = run_and_check(gb, orc, a.row, a.col, a.w, src, flags=base)
+            _, _, off = run_and_check(gb, orc, a.row, a.col, a.w, src, flags=base | gb.F_NO_FUSE)
+            assert on["phases"] < off["phases"], (on["phases"], off["phases"])
 
 
 @pytest.mark.parametrize("delta", [None, 50.0, 1000.0, 1e6])
