@@ -19,10 +19,15 @@
 namespace gbs {
 
 // Who executes a phase: the CTA group (the whole grid for a single-source
-// launch) or one CTA.
+// launch) or one CTA.  Lists are dealt to warps in chunks of 32 entries (one
+// per lane), and the warps of a group are numbered CTA-minor: chunk c goes to
+// CTA c % group_ctas, so a phase of a few thousand entries runs one warp on
+// each of many SMs instead of 32 warps on each of a few (one SM issues every
+// load and atomic of its warps; on the 4096^2 grid, whose buckets start with
+// 1-8 K entries, a bucket took 2 of 152 SMs).
 struct Exec {
-    uint32_t tid, nthreads;   // thread index and count over the executors
-    uint32_t warp, nwarps;    // warp index and count over the executors
+    uint32_t tid, nthreads;   // thread index and count over the executors (vertex loops)
+    uint32_t warp, nwarps;    // warp index (CTA-minor in a group) and count over the executors
 };
 
 __device__ __forceinline__ uint32_t group_rank(const SsspArgs &a) {
@@ -33,7 +38,7 @@ __device__ __forceinline__ Exec group_exec(const SsspArgs &a) {
     Exec x;
     x.tid = group_rank(a) * blockDim.x + threadIdx.x;
     x.nthreads = a.group_ctas * blockDim.x;
-    x.warp = x.tid >> 5;
+    x.warp = (threadIdx.x >> 5) * a.group_ctas + group_rank(a);
     x.nwarps = x.nthreads >> 5;
     return x;
 }
@@ -174,7 +179,7 @@ __device__ void scan_frontier(const SsspArgs &a, const Targets &t, const Exec &x
     uint32_t my_edges = 0;
     uint32_t nc = 0;   // candidates buffered by this warp
     Local loc{kNoLocal, 0u};
-    for (uint32_t base = x.tid - lane; base < count; base += x.nthreads) {
+    for (uint32_t base = x.warp * 32u; base < count; base += x.nthreads) {
         const uint32_t i = base + lane;
         uint32_t u = 0, s = 0, e = 0, he = 0;
         typename Arith<WT>::D du = 0;
@@ -334,7 +339,7 @@ __device__ void rebucket_pending(const SsspArgs &a, const Uniform &U, const Exec
     t.c = c;
     t.fuse = 0;
     uint32_t stale = 0;
-    for (uint32_t base = x.tid - lane_id(); base < count; base += x.nthreads) {
+    for (uint32_t base = x.warp * 32u; base < count; base += x.nthreads) {
         const uint32_t i = base + lane_id();
         int q[1] = {-1};
         uint32_t v[1] = {0};
