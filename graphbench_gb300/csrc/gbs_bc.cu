@@ -54,6 +54,7 @@
 namespace gbs {
 namespace {
 
+constexpr int kBcTPB = 1024;          // threads per CTA of the DAG kernel (one CTA per SM)
 constexpr uint32_t kLaneRow = 32;     // FORWARD / BACKWARD: rows up to this long are walked by one lane
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -719,7 +720,7 @@ __device__ __forceinline__ void finish_rows(const BcArgs &a, uint32_t s0, uint32
 }
 
 template <int WT>
-__global__ void __launch_bounds__(kTPB, 1) bc_dag(BcArgs a) {
+__global__ void __launch_bounds__(kBcTPB, 1) bc_dag(BcArgs a) {
     __shared__ uint32_t s_pub[7];
     __shared__ uint32_t s_nw;
     __shared__ Stage st;
@@ -918,7 +919,7 @@ gbs_status alloc_bc(gbs_graph *g) {
     // in-degrees return to zero at the end of every FORWARD pass
     GBS_CUDA(cudaMemsetAsync(b->indeg, 0, sizeof(uint32_t) * n, g->stream));
     int per_sm = 0;
-    GBS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bc_kernel(g->wtype), kTPB, 0));
+    GBS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bc_kernel(g->wtype), kBcTPB, 0));
     if (per_sm < 1) return fail(GBS_ERR_UNSUPPORTED, "betweenness kernel cannot be resident");
     b->blocks = std::min(per_sm, 1) * g->sms;
     return GBS_OK;
@@ -1030,7 +1031,7 @@ gbs_status run_bc(gbs_graph *g, const uint32_t *sources, uint32_t k, const gbs_p
         GBS_CUDA(cudaEventRecord(e0, s));
         GBS_CUDA(cudaMemsetAsync(b->ctl, 0, sizeof(BcCtl), s));
         GBS_CUDA(cudaMemsetAsync(b->mask, 0, sizeof(uint32_t) * b->mask_words, s));
-        GBS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(b->blocks), dim3(kTPB), args, 0, s));
+        GBS_CUDA(cudaLaunchCooperativeKernel(kfn, dim3(b->blocks), dim3(kBcTPB), args, 0, s));
         GBS_CUDA(cudaEventRecord(e1, s));
         GBS_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;

@@ -37,7 +37,12 @@ constexpr uint32_t kTagInit = 0xFFFFFFFFu;
 constexpr uint32_t kTagPending = 0xFFFFFFFEu;
 constexpr uint32_t kBucketMax = 0xFFFFFF00u;
 constexpr unsigned long long kUnreached = ~0ull;
-constexpr int kTPB = 1024;              // threads per CTA of the persistent kernel
+// Threads per CTA of the persistent SSSP kernels (one CTA per SM): 896
+// leaves 72 registers a thread, and the relaxation no longer spills the way
+// it did at 64 (1024 threads).  Kernel ms, 1024 / 768 / 896 threads: R-MAT 20
+// 1.088 / 1.054 / 1.062, R-MAT 22 2.204 / 2.167 / 2.152, 4096^2 grid
+// 214.6 / 213.2 / 210.0.
+constexpr int kTPB = 896;
 // Default bucket fusion rounds per warp and scan.  Plain width, 4096^2 grid
 // (kernel ms): 1 231, 2 224, 4 240, 8 242; at 64 plain widths 1 96, 2 89,
 // 4 83, 8 80 (the autotuner picks per graph); R-MAT 20 / 22 flat.

@@ -152,7 +152,7 @@ struct Targets {
     uint32_t pend_sel;    // pending list to append to
     WarpScratch *scr;     // this warp's shared-memory scratch
     Ctrs c;               // the list counters (global, or the deciding CTA's shared copy)
-    uint32_t fuse;        // 1: bucket fusion (Local) in this phase
+    uint32_t fuse;        // bucket fusion rounds of this phase (0: none)
 };
 
 // Bucket fusion.  During a scan that relaxes whole rows, a target that

@@ -158,7 +158,7 @@ __device__ __forceinline__ void fuse_drain(const SsspArgs &a, const Targets &t, 
         const uint32_t s = has ? __ldg(a.g.row + u) : 0u;
         const uint32_t e = has ? __ldg(a.g.row + u + 1) : 0u;
         const typename Arith<WT>::D du = loc.d;
-        loc.v = round < a.fuse_rounds ? kNoLocal : kNoKeep;
+        loc.v = round < t.fuse ? kNoLocal : kNoKeep;
         scan_rows<WT>(a, t, u, du, s, e, my_edges, nc, imp, loc);
         cand_drain<WT>(a, t, nc, imp, loc);
     }
@@ -438,7 +438,7 @@ __device__ void run_phase(const SsspArgs &a, const Uniform &U, const Exec &x, Wa
     const bool full = U.full != 0;
     // bucket fusion in whole-row scans (EDGES could not keep the descriptors
     // a kept long row emits: the next scan resets their list)
-    t.fuse = (a.fuse_rounds && full && WT != kWF64 && (U.phase == kPhLightFirst || U.phase == kPhLight)) ? 1u : 0u;
+    t.fuse = (full && WT != kWF64 && (U.phase == kPhLightFirst || U.phase == kPhLight)) ? a.fuse_rounds : 0u;
     // the input size comes with the decision (U.items); the counters are
     // read only where it was not published
     const bool pub = U.items != kNoItems;
