@@ -895,7 +895,10 @@ gbs_status gbs_graph_set_controller(gbs_graph *g, const float *params, uint32_t 
     if (!g->d_mlp) GBS_CUDA(cudaMalloc(&g->d_mlp, sizeof(float) * kMlpFloats));
     GBS_CUDA(cudaMemcpy(g->d_mlp, params, sizeof(float) * kMlpFloats, cudaMemcpyHostToDevice));
     g->mlp_host.assign(params, params + kMlpFloats);
-    g->ctrl_margin = margin > 0 ? margin : 0.10;
+    // default 0.25: on R-MAT 22 single sources spread by about +-10 % around
+    // the learned schedule's mean gain of 3 %, so a tighter limit reverts on
+    // one unlucky source; R-MAT 24 (0.72x) trips it on its first source
+    g->ctrl_margin = margin > 0 ? margin : 0.25;
     g->plain_ms = 0.0;
     g->ctrl_lost = false;
     return GBS_OK;

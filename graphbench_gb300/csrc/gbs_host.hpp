@@ -56,7 +56,7 @@ struct gbs_graph {
     // learned bucket-width controller (gbs_graph_set_controller)
     float *d_mlp = nullptr;
     std::vector<float> mlp_host;
-    double ctrl_margin = 0.10;
+    double ctrl_margin = 0.25;
     double plain_ms = 0.0;        // kernel time of the plain schedule on this graph (the guard)
     bool ctrl_lost = false;       // a learned run lost to plain here: run plain from now on
     // recorded controller inputs (GBS_F_FEATURES)

@@ -353,7 +353,7 @@ gbs_status gbs_trace(gbs_graph *g, gbs_phase_rec *out, uint32_t cap, uint32_t *c
  * None of them grows with the vertex count by itself.
  * params: 5410 floats: input means[16], input scales[16], W1[16][64], b1[64],
  * W2[64][64], b2[64], W3[64][2], b3[2] (row-major, inputs first).  margin
- * (<= 0: 0.10): a learned run that runs longer than (1 + margin) times the
+ * (<= 0: 0.25): a learned run that runs longer than (1 + margin) times the
  * plain schedule on this graph stops and the plain schedule runs instead.  If
  * that plain run finished within the limit (5% timing noise allowed), the
  * controller lost: from then on GBS_F_LEARNED calls on the graph run the plain
