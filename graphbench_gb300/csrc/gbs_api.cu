@@ -895,9 +895,10 @@ gbs_status gbs_graph_set_controller(gbs_graph *g, const float *params, uint32_t 
     if (!g->d_mlp) GBS_CUDA(cudaMalloc(&g->d_mlp, sizeof(float) * kMlpFloats));
     GBS_CUDA(cudaMemcpy(g->d_mlp, params, sizeof(float) * kMlpFloats, cudaMemcpyHostToDevice));
     g->mlp_host.assign(params, params + kMlpFloats);
-    // default 0.25: on R-MAT 22 single sources spread by about +-10 % around
-    // the learned schedule's mean gain of 3 %, so a tighter limit reverts on
-    // one unlucky source; R-MAT 24 (0.72x) trips it on its first source
+    // default 0.25: on R-MAT 22 the learned / plain time of single sources
+    // ranges from 0.71 to 1.27 (16 sources, geometric mean 0.96), so a
+    // tighter limit reverts on one unlucky source of a graph the controller
+    // wins on; R-MAT 24 (geometric mean 1.50) trips it within a few sources
     g->ctrl_margin = margin > 0 ? margin : 0.25;
     g->plain_ms = 0.0;
     g->ctrl_lost = false;
