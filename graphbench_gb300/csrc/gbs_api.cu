@@ -837,9 +837,28 @@ gbs_status gbs_sssp_device(gbs_graph *g, uint32_t source, const gbs_params *para
     return run_sssp(g, source, params, dist_dev, pred_dev, stats);
 }
 
+// The device address of page-locked host memory (gbs_host_alloc,
+// cudaMallocHost, cudaHostRegister), or null for any other pointer.
+static void *device_view(void *host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();   // a pointer the runtime does not know: not an error of the call
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 gbs_status gbs_sssp(gbs_graph *g, uint32_t source, const gbs_params *params, void *dist_out,
                     int32_t *pred_out, gbs_stats *stats) {
     if (!g) return fail(GBS_ERR_INVALID_ARG, "graph is NULL");
+    // page-locked outputs: the unpack kernel writes dist / pred straight into
+    // them over the host link (the run synchronises its stream before it
+    // returns), with no device staging buffer and no copy afterwards
+    void *dist_view = device_view(dist_out);
+    void *pred_view = device_view(pred_out);
+    if ((!dist_out || dist_view) && (!pred_out || pred_view) && (dist_out || pred_out))
+        return run_sssp(g, source, params, dist_view, static_cast<int32_t *>(pred_view), stats);
     gbs_status st = ensure_workspace(g);
     if (st != GBS_OK) return st;
     st = run_sssp(g, source, params, dist_out ? g->d_dist : nullptr, pred_out ? g->d_pred : nullptr,

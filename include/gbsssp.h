@@ -151,8 +151,10 @@ gbs_status gbs_graph_info(const gbs_graph *g, uint32_t *n, uint64_t *m,
                           double *default_delta);
 
 /*
- * One single-source shortest path, outputs in HOST memory (pinned memory from
- * gbs_host_alloc transfers fastest).  dist_out: n uint32 or float32 values in
+ * One single-source shortest path, outputs in HOST memory.  Page-locked
+ * outputs (gbs_host_alloc, cudaMallocHost, cudaHostRegister) are written by
+ * the device directly, with no copy after the run; any other host memory
+ * receives a copy of a device buffer.  dist_out: n uint32 or float32 values in
  * the graph's weight type; pred_out: n int32 values (pred[source] = source,
  * -1 for unreached vertices).  Either output may be NULL.  params and stats
  * may be NULL.  Replaces run_sspath_arr (sssp/csr_sspath_array.c:149), whose

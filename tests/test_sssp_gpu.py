@@ -330,6 +330,36 @@ def test_float64_grid_multi_and_device_outputs(gb, orc):
     assert np.array_equal(dd.cpu().numpy(), D[1]) and np.array_equal(pd.cpu().numpy(), P[1])
 
 
+@pytest.mark.parametrize("wtype", ["u32", "f32", "f64"])
+def test_pinned_host_outputs(wtype, gb, orc):
+    """gbs_sssp writes page-locked host outputs from the device directly and
+    copies into any other host memory.  Pinned, pageable, mixed and single
+    outputs all give the oracle's distances and predecessors."""
+    a = gb.gen_rmat(12, 16, 23)
+    w = {"u32": a.w, "f32": a.w.astype(np.float32) / 3.0, "f64": _fractional(a)}[wtype]
+    src = int(np.argmax(np.diff(a.row.astype(np.int64))))
+    ref = orc.dijkstra(a.row, a.col, w, src)
+    rp = orc.min_tight_pred(a.row, a.col, w, src, ref)
+    with gb.Graph(a.row, a.col, w) as g:
+        hd = gb.PinnedBuffer(a.n, g.dist_dtype)
+        hp = gb.PinnedBuffer(a.n, np.int32)
+        plain_d = np.empty(a.n, dtype=g.dist_dtype)
+        plain_p = np.empty(a.n, dtype=np.int32)
+        for od, op in ((hd.array, hp.array), (plain_d, plain_p), (hd.array, plain_p), (plain_d, hp.array)):
+            od.fill(0)
+            op.fill(0)
+            g.sssp(src, out_dist=od, out_pred=op)
+            assert np.array_equal(od, ref) and np.array_equal(op, rp)
+        hd.array.fill(0)
+        hp.array.fill(0)
+        g.sssp(src, out_dist=hd.array, want_pred=False)
+        assert np.array_equal(hd.array, ref) and not hp.array.any()
+        g.sssp(src, want_dist=False, out_pred=hp.array)
+        assert np.array_equal(hp.array, rp)
+        hd.free()
+        hp.free()
+
+
 def test_reference_mirror_fractional_weights(gb, orc, ref_serial):
     """The Python mirror with fractional double weights returns the
     reference's own run_sspath_arr doubles bit for bit."""
