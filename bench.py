@@ -247,7 +247,7 @@ def arm_learned(gb, g, order, W, K, par=None):
 
 def arm_autotuned(gb, g, order, W, K, srcs, par=None):
     t0 = time.time()
-    kw, rep = g.autotune([int(s) for s in srcs[:4]], budget_ms=3000)
+    kw, rep = g.autotune([int(s) for s in srcs[:8]], budget_ms=3000)
     tune_s = time.time() - t0
     if par is not None:
         par.equal("arms", "plain (autotuned schedule)", g.sssp(order[W], **kw)[:2], g.sssp(order[W])[:2])
