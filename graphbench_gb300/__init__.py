@@ -535,7 +535,7 @@ class Graph:
         _check(lib.gbs_autotune(self._h, _ptr(src), len(src), float(budget_ms), ctypes.byref(rep)), "gbs_autotune")
         b = rep.best
         kw = {"delta": b.delta, "light": b.light, "solo_entries": b.solo_entries, "solo_descs": b.solo_descs,
-              "inline_edges": b.inline_edges, "fuse_rounds": b.fuse_rounds}
+              "inline_edges": b.inline_edges, "fuse_rounds": b.fuse_rounds, "full_items": b.full_items}
         r = {k: getattr(rep, k) for k, _ in TuneReport._fields_ if k != "best"}
         r["best"] = dict(kw)
         return kw, r

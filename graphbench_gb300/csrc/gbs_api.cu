@@ -536,7 +536,7 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dis
     a.no_heavy = (g->wtype == GBS_WEIGHT_F64 ? r.light >= g->max_w
                                              : r.light_bits >= max_weight_bits(g->wtype, g->max_w)) ? 1u : 0u;
     a.inline_max = (p && p->inline_edges) ? p->inline_edges : kInlineEdges;
-    a.full_items = (p && p->full_items) ? p->full_items : default_full_items(g->n);
+    a.full_items = (p && p->full_items) ? p->full_items : std::max(g->n, kFullItems);
     a.fuse_rounds = (a.flags & GBS_F_NO_FUSE) ? 0u : ((p && p->fuse_rounds) ? p->fuse_rounds : kFuseRounds);
     a.run_ns = a.wait_ns * 16ull;
     a.ctrl = learned ? kCtrlLearned : kCtrlFixed;

@@ -199,7 +199,7 @@ gbs_status build_plan(gbs_plan *p, const gbs_batch_params *bp, int sms, uint32_t
     a.wait_ns = (unsigned long long)((bp && bp->wait_limit_ms) ? bp->wait_limit_ms : 4000u) * 1000000ull;
     a.run_ns = a.wait_ns * 16ull;
     a.inline_max = (bp && bp->inline_edges) ? bp->inline_edges : kInlineEdges;
-    a.full_items = default_full_items(n_cap);
+    a.full_items = split_full_items(n_cap);
     a.group_ctas = gc;
     a.inst = p->d_inst;
     a.res = p->d_res;

@@ -54,15 +54,18 @@ enum Phase : uint32_t {
 constexpr int kUnroll = 4;
 constexpr uint32_t kDescEdges = 32u * kUnroll;   // edges per descriptor (one warp round)
 constexpr uint32_t kInlineEdges = 32u;           // default inline_max: rows up to this long are relaxed in SCAN
-constexpr uint32_t kFullItems = 1024u;           // least default full_items
-// Default full_items of a graph of n vertices: a bucket whose lists hold at
-// most max(1024, n / 16) entries when it starts relaxes whole rows.  Its
-// heavy edges are then relaxed by its light scans instead of a heavy phase of
-// their own (a grid step fewer per bucket; a vertex scanned again in the
-// bucket relaxes them again).  Measured with the plain width (kernel ms):
-// R-MAT 20 1.40 at 1024 -> 1.21 at n / 16; R-MAT 22 2.56 -> 2.29 (n / 16);
-// 1024^2 grid 51.2 -> 49.2 (flat from 4096 up).
-inline uint32_t default_full_items(uint32_t n) { return n / 16u > kFullItems ? n / 16u : kFullItems; }
+constexpr uint32_t kFullItems = 1024u;           // least split threshold
+// A bucket whose lists hold at most full_items entries when it starts relaxes
+// whole rows: its heavy edges go through its light scans instead of a heavy
+// phase of their own (a grid step fewer per bucket; a vertex scanned again
+// in the bucket relaxes them again).  split_full_items is the threshold that
+// keeps the light/heavy split for the large buckets, max(1024, n / 16); the
+// single-source default is every bucket (n).  Measured with the plain width
+// (kernel ms), before bucket fusion: R-MAT 20 1.40 at 1024 -> 1.21 at n / 16,
+// R-MAT 22 2.56 -> 2.29; with fusion and 896 threads, n / 16 -> every bucket:
+// R-MAT 20 1.059 -> 1.080, R-MAT 22 2.142 -> 2.002, R-MAT 24 7.57 -> 6.88,
+// 4096^2 grid 209.6 -> 209.7.
+inline uint32_t split_full_items(uint32_t n) { return n / 16u > kFullItems ? n / 16u : kFullItems; }
 
 // Values identical in every CTA (the kernel's uniform state).
 struct Uniform {

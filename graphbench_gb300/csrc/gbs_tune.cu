@@ -82,9 +82,10 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
     gbs_params best = base;
     best.delta = d0;
     double best_scale = 1.0;
-    bool best_nosplit = false;
-    // 1. width for each split: coarse exponents, then the neighbours of the
-    //    best one (one and two steps on each side, twice)
+    bool best_nosplit = true;   // the default relaxes every bucket whole
+    // 1. width with and without the light/heavy split of the large buckets:
+    //    coarse exponents, then the neighbours of the best one (one and two
+    //    steps on each side, twice)
     for (int split = 0; split < 2 && b.left(); ++split) {
         std::vector<std::pair<int, double>> seen;   // (exponent, ms)
         auto eval = [&](int e) -> gbs_status {
@@ -97,7 +98,7 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
             } else {
                 gbs_params p = base;
                 p.delta = d0 * std::ldexp(1.0, e);
-                p.light = split ? INFINITY : -1.0;
+                if (split) p.full_items = split_full_items(g->n);
                 gbs_status r = time_single(g, src, p, b, out->runs, ms);
                 if (r != GBS_OK) return r;
                 ++out->candidates;
@@ -105,7 +106,7 @@ gbs_status gbs_autotune(gbs_graph *g, const uint32_t *sources, uint32_t count, d
                     best_ms = ms;
                     best = p;
                     best_scale = std::ldexp(1.0, e);
-                    best_nosplit = split != 0;
+                    best_nosplit = split == 0;
                 }
             }
             seen.push_back({e, ms});

@@ -80,8 +80,10 @@ typedef struct gbs_params {
                                 descriptors relaxed one warp each; 0 = 32 */
     uint32_t full_items;     /* a bucket whose lists hold at most this many entries
                                 when it starts relaxes whole rows (light and heavy
-                                edges together, no heavy phase); 0 = max(1024,
-                                vertices / 16) */
+                                edges together, no heavy phase); 0 = every bucket,
+                                so the light bound only shapes runs that set this
+                                (max(1024, vertices / 16) keeps the split for the
+                                large buckets; batched plans always use that) */
     uint32_t fuse_rounds;    /* bucket fusion: a whole-row scan relaxes the vertices
                                 it improves into the current bucket itself, for up
                                 to this many rounds per warp, before the next ones

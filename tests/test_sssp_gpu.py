@@ -99,16 +99,20 @@ def test_hub_rows_split_into_descriptors(gb, orc):
     run_and_check(gb, orc, a.row, a.col, a.w, src, delta=100000)
 
 
-@pytest.mark.parametrize("mode", ["grid_only", "default", "all_solo", "all_solo_no_fuse", "no_fuse"])
+@pytest.mark.parametrize("mode", ["grid_only", "default", "all_solo", "all_solo_no_fuse", "no_fuse", "split",
+                                  "all_solo_split"])
 def test_solo_phases_same_result(mode, gb, orc):
     """Phases run by one CTA (small inputs) or by the whole grid give the same
     result; 'all_solo' makes every phase after the first run on one CTA;
-    the no_fuse modes turn bucket fusion off."""
+    the no_fuse modes turn bucket fusion off; the split modes keep the
+    light/heavy split in every bucket (heavy phases)."""
     kw = {"grid_only": dict(flags=gb.F_NO_SOLO),
           "default": {},
           "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30),
           "all_solo_no_fuse": dict(solo_entries=1 << 30, solo_descs=1 << 30, flags=gb.F_NO_FUSE),
-          "no_fuse": dict(flags=gb.F_NO_FUSE)}[mode]
+          "no_fuse": dict(flags=gb.F_NO_FUSE),
+          "split": dict(full_items=1),
+          "all_solo_split": dict(solo_entries=1 << 30, solo_descs=1 << 30, full_items=1)}[mode]
     a = gb.gen_rmat(13, 16, 11)
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
     _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, **kw)
@@ -128,17 +132,18 @@ def test_solo_phases_same_result(mode, gb, orc):
         assert st3["pending_scans"] >= 1
 
 
-@pytest.mark.parametrize("full_items", [1, 0, 1 << 30])
+@pytest.mark.parametrize("full_items", [1, 1024, 0, 1 << 30])
 def test_whole_row_threshold_same_result(full_items, gb, orc):
     """Buckets of up to full_items entries relax whole rows (0: the default,
-    max(1024, n / 16)); 1 splits every bucket but the source's, 2^30 relaxes
-    every bucket whole.  Distances and predecessors stay the oracle's, and on
-    R-MAT the heavy phases disappear when every bucket is whole."""
+    every bucket); 1 splits every bucket but the source's, 1024 the large
+    ones, 2^30 relaxes every bucket whole.  Distances and predecessors stay
+    the oracle's, and on R-MAT the heavy phases disappear when every bucket
+    is whole."""
     a = gb.gen_rmat(14, 16, 21)
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
     _, _, st = run_and_check(gb, orc, a.row, a.col, a.w, src, full_items=full_items)
     _, _, st1 = run_and_check(gb, orc, a.row, a.col, a.w, src, full_items=1)
-    if full_items == 1 << 30:
+    if full_items in (0, 1 << 30):
         assert st["phases"] < st1["phases"]
     g2 = gb.gen_grid(48, 80, 7, "f32")
     run_and_check(gb, orc, g2.row, g2.col, g2.w, 0, full_items=full_items)
@@ -190,7 +195,7 @@ def test_pending_list_small_delta(gb, orc):
     assert st["pending_scans"] >= 1
 
 
-@pytest.mark.parametrize("mode", ["default", "all_solo", "no_fuse"])
+@pytest.mark.parametrize("mode", ["default", "all_solo", "no_fuse", "split"])
 def test_pending_rebucketing_on_one_cta(mode, gb, orc):
     """Widths far below the largest weight push most vertices past the ring
     window; their re-bucketing runs on the deciding CTA when the pending list
@@ -198,7 +203,7 @@ def test_pending_rebucketing_on_one_cta(mode, gb, orc):
     (before the re-bucketing fenced its tag stores and the pending minimum,
     half of these runs on one CTA stopped early or skipped vertices)."""
     kw = {"default": {}, "all_solo": dict(solo_entries=1 << 30, solo_descs=1 << 30),
-          "no_fuse": dict(flags=gb.F_NO_FUSE)}[mode]
+          "no_fuse": dict(flags=gb.F_NO_FUSE), "split": dict(full_items=1)}[mode]
     cases = [(gb.gen_grid(54, 83, 107, "u32"), [1, 2, 3]), (gb.gen_grid(47, 71, 205, "f32"), [2.0, 20.0]),
              (gb.gen_rmat(12, 16, 302), [1, 4])]
     pend = 0
