@@ -180,11 +180,14 @@ def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: in
         fin = np.sort(fin.astype(np.float64))
         settled = lambda dd: np.searchsorted(fin, dd, side="left").astype(np.float64)
         g.sssp_device(src)
+        # split 1: the light/heavy split at the width in every bucket above
+        # max(1024, n / 16) entries (the fixed schedule's split rule)
+        split_items = max(1024, host.n // 16)
         for k in sweep_k:
             for split in (0, 1):
-                light = None if split else math.inf
-                g.sssp_device(src, delta=d * 2.0 ** k, light=light)          # warm-up
-                st = g.sssp_device(src, delta=d * 2.0 ** k, light=light, flags=gb.F_TRACE | gb.F_FEATURES)
+                kw = dict(light=None, full_items=split_items) if split else dict(light=math.inf)
+                g.sssp_device(src, delta=d * 2.0 ** k, **kw)          # warm-up
+                st = g.sssp_device(src, delta=d * 2.0 ** k, flags=gb.F_TRACE | gb.F_FEATURES, **kw)
                 tr = g.trace()
                 x = g.features()
                 runs[(k, split)] = (bucket_curve(tr, st["delta_used"]), x, st["kernel_ms"])
@@ -228,7 +231,7 @@ def collect_graph(spec: dict, sweep_k=SWEEP_K, horizon: float = HORIZON, cap: in
     w = np.concatenate([[1.0], w / w.sum()])
     return {"spec": spec, "x": x.astype(np.float32), "t": t, "w": (w / w.sum()).astype(np.float32),
             "best_fixed": {"k": best_fixed[0], "split": best_fixed[1], "ms": total[best_fixed],
-                           "plain_ms": total[(0, 1)]}}
+                           "plain_ms": total[(0, 0)]}}
 
 
 def dataset(collected: list[dict]):
