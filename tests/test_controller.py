@@ -199,7 +199,7 @@ def test_learned_guard_longer_source_is_not_a_loss(gb, orc):
 @pytest.mark.gpu
 def test_trained_controller_beats_plain_on_held_out_graphs(gb):
     """The committed controller on graphs and seeds outside its training set
-    (a 768^2 grid, R-MAT 18 and R-MAT 20, the largest training scale): total
+    (a 768^2 grid, R-MAT 18 and R-MAT 20 with held-out seeds): total
     kernel time of learned runs below the plain fixed delta's (a call whose
     learned run fell back is charged both runs)."""
     cases = [(gb.gen_grid(768, 768, 97, "f32"), [0]), (gb.gen_rmat(18, 16, 77), None),
@@ -217,6 +217,24 @@ def test_trained_controller_beats_plain_on_held_out_graphs(gb):
                     plain += a["kernel_ms"]
                     learned += b["kernel_ms"]   # includes any abandoned run
             assert learned < plain, (host.n, learned, plain)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("spec", [{"kind": "rmat", "scale": 12, "seed": 41}, {"kind": "grid", "side": 128, "seed": 42}])
+def test_collect_graph_labels(spec, gb):
+    """collect_graph: every (width, split) schedule of a small sweep runs with
+    its trace and inputs; the samples are the initial state plus one per
+    recorded bucket start, the width labels come from the sweep, the split
+    labels are 0 / 1, and the weights sum to 1."""
+    from graphbench_gb300 import controller
+    c = controller.collect_graph(spec, sweep_k=(-1, 0, 1, 2), cap=500, seed=3)
+    x, t, w = c["x"], c["t"], c["w"]
+    assert x.shape[1] == gb.N_FEAT and len(x) == len(t) == len(w) >= 2
+    assert set(np.unique(t[1:, 0])) <= {-1.0, 0.0, 1.0, 2.0}
+    assert set(np.unique(t[:, 1])) <= {0.0, 1.0}
+    assert abs(float(w.sum()) - 1.0) < 1e-5 and (w >= 0).all()
+    bf = c["best_fixed"]
+    assert bf["k"] in (-1, 0, 1, 2) and bf["split"] in (0, 1) and 0 < bf["ms"] <= bf["plain_ms"] * 1.5
 
 
 @pytest.mark.gpu
