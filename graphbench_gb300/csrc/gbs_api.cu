@@ -547,7 +547,9 @@ gbs_status launch_run(gbs_graph *g, uint32_t src, const gbs_params *p, void *dis
     a.guard_ns = (learned && g->plain_ms > 0)
                      ? (unsigned long long)(g->plain_ms * (1.0 + g->ctrl_margin) * 1e6)
                      : 0ull;
-    if (!learned || a.no_heavy) full0 = a.no_heavy;
+    // the source's bucket holds one entry: whole rows under the fixed
+    // schedule's rule (full_items >= 1), as every later bucket of that size
+    if (!learned || a.no_heavy) full0 = (a.no_heavy || (!learned && a.full_items >= 1u)) ? 1u : 0u;
     if (a.flags & GBS_F_FEATURES) {
         if (!g->d_feat) {
             g->feat_cap = 1u << 18;

@@ -51,9 +51,10 @@ def test_known_answer(case, gb):
     mg = _mg()
     row, col, w = mg.to_csr(case)
     with gb.Graph(row, col, w) as g:
-        d, p, _ = g.sssp(case["source"], delta=case["delta"])
-    assert np.array_equal(d, mg.expected_dist(case))
-    assert p.tolist() == case["pred"]
+        for kw in ({}, dict(full_items=1)):   # whole rows / the split in every bucket
+            d, p, _ = g.sssp(case["source"], delta=case["delta"], **kw)
+            assert np.array_equal(d, mg.expected_dist(case)), kw
+            assert p.tolist() == case["pred"], kw
 
 
 @pytest.mark.parametrize("case", SEEDED, ids=[c["name"] for c in SEEDED])
@@ -71,9 +72,12 @@ def test_seeded_golden(case, gb):
 @pytest.mark.parametrize("delta,light", [(None, None), (1, None), (3, None), (40, None), (255, None),
                                          (10000, None), (8, 0), (8, 64), (2, 300)])
 def test_rmat_deltas_and_splits(delta, light, gb, orc):
+    """Widths and light bounds, with whole rows in every bucket (the default)
+    and with the split in every bucket (full_items 1)."""
     a = gb.gen_rmat(13, 16, 3)
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
     run_and_check(gb, orc, a.row, a.col, a.w, src, delta=delta, light=light)
+    run_and_check(gb, orc, a.row, a.col, a.w, src, delta=delta, light=light, full_items=1)
 
 
 def test_rmat16_many_sources_one_graph(gb, orc):
@@ -179,7 +183,7 @@ def test_split_covering_all_edges_skips_heavy(wtype, gb, orc):
     wmax = float(a.w.max())
     with gb.Graph.from_host(a) as g:
         for light, heavy_expected in [(wmax, False), (wmax * 4, False), (wmax - 1, True)]:
-            d, p, st = g.sssp(src, delta=wmax / 8, light=light, flags=gb.F_TRACE)
+            d, p, st = g.sssp(src, delta=wmax / 8, light=light, flags=gb.F_TRACE, full_items=1)
             kinds = {r["kind"] for r in g.trace()}
             assert ("heavy" in kinds) == heavy_expected, (light, kinds)
             ref = orc.dijkstra(a.row, a.col, a.w, src)
@@ -313,6 +317,7 @@ def test_float64_rmat_deltas_and_splits(delta, light, gb, orc):
     src = int(np.argmax(np.diff(a.row.astype(np.int64))))
     d, p, st = run_and_check(gb, orc, a.row, a.col, w, src, delta=delta, light=light)
     assert d.dtype == np.float64 and st["reached"] == int(np.isfinite(d).sum())
+    run_and_check(gb, orc, a.row, a.col, w, src, delta=delta, light=light, full_items=1)
 
 
 def test_float64_grid_multi_and_device_outputs(gb, orc):
